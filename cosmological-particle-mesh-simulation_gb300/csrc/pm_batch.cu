@@ -1,0 +1,622 @@
+// C ABI: resident batch engine (pm_batch_*).
+//
+// Simulations are resident in HBM.  Particles of all simulations live in one set of
+// structure-of-arrays buffers (double buffered), stored as float32 displacements from
+// their Lagrangian lattice point plus the particle index; every step the kick writes
+// the state back in the order of the step's cell-key sort, so that the next step reads
+// it almost in order.  Simulation s owns the slot range [part_off_s, part_off_s + np_s)
+// and the x-rows [row_base_s, row_base_s + N_s^2) of the common key space, in the same
+// order, so one radix sort serves the whole batch.  Every phase is one persistent launch
+// over all simulations (the spectral phases: one per distinct grid size).  A step is
+// captured once into a CUDA graph per plan and replayed; the scale factor and the
+// step coefficients advance on the device.
+#include <algorithm>
+#include <map>
+#include <memory>
+
+#include "pm_host.cuh"
+
+using namespace pm;
+
+namespace {
+
+struct SimRec {
+  int id = 0;
+  pm_config cfg{};
+  int n = 0, np1 = 0;
+  long long np = 0;
+  int nsteps = 0, done = 0;
+  double a = 0.0, da = 0.0;
+  bool resident = false;  // particles in the batch arrays
+  DBuf grid, spec, rho;   // potential (and density unless keep_density), spectrum, density
+  DBuf fin_pos, fin_vel;  // final state once retired (absolute, particle order)
+  long long part_off = 0;
+  unsigned row_base = 0;
+};
+
+enum Phase { PH_KEYS = 0, PH_DEP, PH_KICK, PH_FIXED };
+
+struct Plan {
+  int nsims = 0;
+  long long ptot = 0;
+  unsigned rows = 0;
+  int xbits = 0, bits = 0;
+  std::vector<int> sizes;  // distinct grid sizes
+  int fixed_total[PH_FIXED]{};
+  std::vector<int> x_total, line_total;  // per distinct size
+  int max_dep_smem = 0;
+};
+
+const int kStateArrays = 7;
+
+}  // namespace
+
+struct pm_batch {
+  int device = 0, sms = 1;
+  size_t cap = 0;
+  std::vector<std::unique_ptr<SimRec>> sims;  // resident, in slot order
+  std::vector<std::unique_ptr<SimRec>> retired;
+  std::map<int, std::unique_ptr<Tables>> tables;
+  std::map<long long, std::unique_ptr<Lattice>> lattices;
+  int next_id = 1;
+  // particle state, two copies; arrays x y z vx vy vz id
+  DBuf st[2][kStateArrays];
+  long long pcap = 0;
+  int cur = 0;
+  SortBufs sort;
+  DBuf row_start, d_sims, d_prefix, d_err;
+  Plan plan;
+  bool dirty = true, keys_valid = false;
+  bool graphs = true;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  cudaStream_t own = nullptr;  // used when the caller passes the legacy stream (captures need one)
+  std::string err;
+};
+
+namespace {
+
+int bfail(pm_batch* b, int code, const std::string& m) {
+  if (b) b->err = m;
+  return code;
+}
+
+int bcuda(pm_batch* b, cudaError_t e, const char* where) {
+  return bfail(b, e == cudaErrorMemoryAllocation ? PM_ERR_OOM : PM_ERR_CUDA,
+               std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define PB_CK(call, where)                                  \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return bcuda(b, e_, where);      \
+  } while (0)
+
+Parts state(pm_batch* b, int which) {
+  Parts p;
+  p.x = b->st[which][0].as<float>();
+  p.y = b->st[which][1].as<float>();
+  p.z = b->st[which][2].as<float>();
+  p.vx = b->st[which][3].as<float>();
+  p.vy = b->st[which][4].as<float>();
+  p.vz = b->st[which][5].as<float>();
+  p.id = b->st[which][6].as<unsigned>();
+  return p;
+}
+
+long long resident_particles(pm_batch* b) {
+  long long t = 0;
+  for (auto& s : b->sims) t += s->np;
+  return t;
+}
+
+size_t footprint(const pm_config& c) {
+  const size_t n = c.n_cells;
+  const size_t np = (size_t)c.n_parts * c.n_parts * c.n_parts;
+  size_t f = n * n * n * sizeof(float);                          // potential / density
+  if (c.flags & PM_FLAG_KEEP_DENSITY) f += n * n * n * sizeof(float);
+  f += n * n * (size_t)spec_pitch((int)n) * sizeof(float2);      // spectrum
+  f += np * (2 * kStateArrays * 4 + 4 * 4);                      // state x2, keys/vals x2
+  f += np * 6 * sizeof(float);                                   // final state
+  f += n * n * sizeof(unsigned) + 4096;                          // row starts, tables
+  return f;
+}
+
+size_t used_bytes(pm_batch* b) {
+  size_t u = 0;
+  for (auto& s : b->sims) u += footprint(s->cfg);
+  for (auto& s : b->retired) u += (size_t)s->np * 6 * sizeof(float);
+  return u;
+}
+
+cudaError_t grow_state(pm_batch* b, long long need, cudaStream_t st) {
+  if (need <= b->pcap) return cudaSuccess;
+  long long cap = std::max(need, b->pcap + b->pcap / 2);
+  const long long keep = resident_particles(b);
+  for (int w = 0; w < 2; ++w) {
+    for (int k = 0; k < kStateArrays; ++k) {
+      DBuf nb;
+      cudaError_t e = nb.ensure((size_t)cap * 4);
+      if (e) return e;
+      if (w == b->cur && keep > 0 && b->st[w][k].p) {
+        e = cudaMemcpyAsync(nb.p, b->st[w][k].p, (size_t)keep * 4, cudaMemcpyDeviceToDevice, st);
+        if (e) return e;
+        e = cudaStreamSynchronize(st);
+        if (e) return e;
+      }
+      b->st[w][k].release();
+      b->st[w][k] = nb;
+    }
+  }
+  b->pcap = cap;
+  return b->sort.ensure(cap);
+}
+
+void drop_graphs(pm_batch* b) {
+  for (auto& g : b->gexec) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+}
+
+Tables* tables_for(pm_batch* b, int n) {
+  auto& t = b->tables[n];
+  if (!t) t.reset(new Tables());
+  return t.get();
+}
+
+Lattice* lattice_for(pm_batch* b, int np1, int n) {
+  auto& l = b->lattices[((long long)np1 << 32) | (unsigned)n];
+  if (!l) l.reset(new Lattice());
+  return l.get();
+}
+
+// Build the plan (Sim descriptors, work prefixes) for the resident simulations.
+int build_plan(pm_batch* b, cudaStream_t st) {
+  Plan& P = b->plan;
+  P = Plan();
+  P.nsims = (int)b->sims.size();
+  if (P.nsims == 0) return PM_OK;
+  int nmax = 0;
+  for (auto& s : b->sims) nmax = std::max(nmax, s->n);
+  P.xbits = ceil_log2(nmax);
+  std::vector<Sim> hs(P.nsims);
+  const int S = P.nsims;
+  std::vector<int> pre;  // [phase][S+1]
+  long long off = 0;
+  unsigned rows = 0;
+  for (int i = 0; i < S; ++i) {
+    SimRec& r = *b->sims[i];
+    r.part_off = off;
+    r.row_base = rows;
+    off += r.np;
+    rows += (unsigned)((long long)r.n * r.n);
+    if (std::find(P.sizes.begin(), P.sizes.end(), r.n) == P.sizes.end()) P.sizes.push_back(r.n);
+  }
+  P.ptot = off;
+  P.rows = rows;
+  P.bits = ceil_log2((long long)rows) + P.xbits;
+  if (P.bits > 32) return bfail(b, PM_ERR_ADMIT, "batch key space exceeds 32 bits");
+  std::sort(P.sizes.begin(), P.sizes.end());
+  const int nph = PH_FIXED + 2 * (int)P.sizes.size();
+  pre.assign((size_t)nph * (S + 1), 0);
+  auto at = [&](int ph, int s) -> int& { return pre[(size_t)ph * (S + 1) + s]; };
+  for (int i = 0; i < S; ++i) {
+    SimRec& r = *b->sims[i];
+    Sim& d = hs[i];
+    d = Sim();
+    d.n = r.n;
+    d.pitch = spec_pitch(r.n);
+    d.np1 = r.np1;
+    d.xbits = P.xbits;
+    d.ty = TILE_Y;
+    d.tz = TILE_Z;
+    d.np = r.np;
+    d.part_off = r.part_off;
+    d.row_base = r.row_base;
+    d.phi = r.grid.as<float>();
+    d.rho = (r.cfg.flags & PM_FLAG_KEEP_DENSITY) ? r.rho.as<float>() : r.grid.as<float>();
+    d.spec = r.spec.as<float2>();
+    Tables* t = tables_for(b, r.n);
+    d.s2 = t->s2.as<float>();
+    d.tw = t->tw.as<float2>();
+    Lattice* l = lattice_for(b, r.np1, r.n);
+    d.q_int = l->qi.as<int>();
+    d.q_frac = l->qf.as<float>();
+    d.mass_scale = (float)(std::pow((double)r.n / r.np1, 3) / (double)(1u << PM_FIX_BITS));
+    d.a = r.a;
+    d.da = r.da;
+    d.om = r.cfg.omega_m0;
+    d.ol = r.cfg.omega_lambda0;
+    d.ok = r.cfg.omega_k0;
+    d.h0 = r.cfg.h0;
+    d.step = r.done;
+    d.nsteps = r.nsteps;
+    d.active = 1;
+    d.fix_f = (r.cfg.flags & PM_FLAG_FIX_COSMO_F) ? 1 : 0;
+    at(PH_KEYS, i + 1) = at(PH_KEYS, i) + (int)((r.np + 255) / 256);
+    at(PH_DEP, i + 1) = at(PH_DEP, i) + (r.n / TILE_Y) * (r.n / TILE_Z);
+    at(PH_KICK, i + 1) = at(PH_KICK, i) + (int)((r.np + 255) / 256);
+    for (size_t g = 0; g < P.sizes.size(); ++g) {
+      const bool mine = P.sizes[g] == r.n;
+      const int phx = PH_FIXED + 2 * (int)g, phl = phx + 1;
+      at(phx, i + 1) = at(phx, i) + (mine ? (int)spectral_units(SPEC_X_R2C, r.n) : 0);
+      at(phl, i + 1) = at(phl, i) + (mine ? (int)spectral_units(SPEC_Y_FWD, r.n) : 0);
+    }
+    P.max_dep_smem = std::max(P.max_dep_smem, (int)deposit_smem_bytes(r.n, TILE_Y, TILE_Z));
+  }
+  for (int ph = 0; ph < PH_FIXED; ++ph) P.fixed_total[ph] = at(ph, S);
+  for (size_t g = 0; g < P.sizes.size(); ++g) {
+    P.x_total.push_back(at(PH_FIXED + 2 * (int)g, S));
+    P.line_total.push_back(at(PH_FIXED + 2 * (int)g + 1, S));
+  }
+  PB_CK(b->d_sims.ensure(sizeof(Sim) * S), "alloc sims");
+  PB_CK(b->d_prefix.ensure(sizeof(int) * pre.size()), "alloc prefix");
+  PB_CK(b->row_start.ensure(sizeof(unsigned) * ((size_t)rows + 1)), "alloc rows");
+  PB_CK(cudaMemcpyAsync(b->d_sims.p, hs.data(), sizeof(Sim) * S, cudaMemcpyHostToDevice, st), "upload sims");
+  PB_CK(cudaMemcpyAsync(b->d_prefix.p, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, st),
+        "upload prefix");
+  PB_CK(launch_coef(b->d_sims.as<Sim>(), S, 0, st), "coef");
+  PB_CK(cudaStreamSynchronize(st), "plan sync");
+  for (int n : P.sizes) PB_CK(spectral_dispatch(SPEC_PREPARE, n, nullptr, Work(), 0, st), "prepare");
+  PB_CK(deposit_prepare(), "prepare deposit");
+  drop_graphs(b);
+  b->dirty = false;
+  return PM_OK;
+}
+
+Work work_of(pm_batch* b, int ph, int total) {
+  Work w;
+  w.prefix = b->d_prefix.as<int>() + (size_t)ph * (b->plan.nsims + 1);
+  w.nsims = b->plan.nsims;
+  w.total = total;
+  return w;
+}
+
+// Enqueue one step (state in b->st[cur] -> b->st[1 - cur]).
+int enqueue_step(pm_batch* b, int cur, cudaStream_t st) {
+  Plan& P = b->plan;
+  const Sim* ds = b->d_sims.as<Sim>();
+  int* err = b->d_err.as<int>();
+  Parts in = state(b, cur), out = state(b, 1 - cur);
+  bool alt = false;
+  PB_CK(radix_sort(b->sort.keys.as<unsigned>(), b->sort.vals.as<unsigned>(), P.ptot, P.bits, true,
+                   b->sort.scratch(), &alt, st),
+        "sort");
+  unsigned* perm = alt ? b->sort.vals_alt.as<unsigned>() : b->sort.vals.as<unsigned>();
+  unsigned* skeys = alt ? b->sort.keys_alt.as<unsigned>() : b->sort.keys.as<unsigned>();
+  PB_CK(launch_row_start(skeys, P.ptot, P.xbits, P.rows, b->row_start.as<unsigned>(), st), "rows");
+  PB_CK(launch_deposit(ds, work_of(b, PH_DEP, P.fixed_total[PH_DEP]), in, perm, b->row_start.as<unsigned>(),
+                       POS_DISP, err, grid_for(P.fixed_total[PH_DEP], b->sms, 8), P.max_dep_smem, st),
+        "deposit");
+  const SpecKind order[5] = {SPEC_X_R2C, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Y_INV, SPEC_X_C2R};
+  for (SpecKind k : order) {
+    for (size_t g = 0; g < P.sizes.size(); ++g) {
+      const bool xk = (k == SPEC_X_R2C || k == SPEC_X_C2R);
+      const int ph = PH_FIXED + 2 * (int)g + (xk ? 0 : 1);
+      const int tot = xk ? P.x_total[g] : P.line_total[g];
+      PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot), grid_for(tot, b->sms, 8), st), "spectral");
+    }
+  }
+  PB_CK(launch_kick(ds, work_of(b, PH_KICK, P.fixed_total[PH_KICK]), in, out, perm, b->sort.keys.as<unsigned>(),
+                    POS_DISP, err, grid_for(P.fixed_total[PH_KICK], b->sms, 16), st),
+        "kick");
+  PB_CK(launch_coef(b->d_sims.as<Sim>(), P.nsims, 1, st), "coef");
+  return PM_OK;
+}
+
+int ensure_keys(pm_batch* b, cudaStream_t st) {
+  if (b->keys_valid) return PM_OK;
+  Plan& P = b->plan;
+  PB_CK(launch_keys_disp(b->d_sims.as<Sim>(), work_of(b, PH_KEYS, P.fixed_total[PH_KEYS]), state(b, b->cur),
+                         b->sort.keys.as<unsigned>(), nullptr, b->d_err.as<int>(),
+                         grid_for(P.fixed_total[PH_KEYS], b->sms, 16), st),
+        "keys");
+  b->keys_valid = true;
+  return PM_OK;
+}
+
+int run_steps(pm_batch* b, int k, cudaStream_t st) {
+  for (int i = 0; i < k; ++i) {
+    const int cur = b->cur;
+    if (b->graphs) {
+      if (!b->gexec[cur]) {
+        cudaGraph_t g = nullptr;
+        PB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+        const int r = enqueue_step(b, cur, st);
+        const cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (r) {
+          if (g) cudaGraphDestroy(g);
+          return r;
+        }
+        PB_CK(e, "end capture");
+        cudaError_t ie = cudaGraphInstantiate(&b->gexec[cur], g, 0);
+        cudaGraphDestroy(g);
+        PB_CK(ie, "instantiate");
+      }
+      PB_CK(cudaGraphLaunch(b->gexec[cur], st), "graph launch");
+    } else {
+      if (int r = enqueue_step(b, cur, st)) return r;
+    }
+    b->cur = 1 - cur;
+  }
+  return PM_OK;
+}
+
+// Copy the final state of finished simulations out and compact the others.
+int retire_finished(pm_batch* b, cudaStream_t st) {
+  bool any = false;
+  for (auto& s : b->sims) any |= s->done >= s->nsteps;
+  if (!any) return PM_OK;
+  Parts curp = state(b, b->cur);
+  std::vector<std::unique_ptr<SimRec>> keep;
+  long long off = 0;
+  const int dst = 1 - b->cur;
+  for (auto& s : b->sims) {
+    if (s->done >= s->nsteps) {
+      const size_t pb = (size_t)3 * s->np * sizeof(float);
+      PB_CK(s->fin_pos.ensure(pb), "alloc final");
+      PB_CK(s->fin_vel.ensure(pb), "alloc final");
+      Lattice* l = lattice_for(b, s->np1, s->n);
+      PB_CK(launch_disp_to_abs(curp, s->part_off, s->np, s->np1, s->n, l->qi.as<int>(), l->qf.as<float>(),
+                               s->fin_pos.as<float>(), s->fin_vel.as<float>(), st),
+            "extract");
+      s->resident = false;
+      s->grid.release();
+      s->spec.release();
+      s->rho.release();
+      b->retired.push_back(std::move(s));
+    } else {
+      for (int k = 0; k < kStateArrays; ++k)
+        PB_CK(cudaMemcpyAsync(b->st[dst][k].as<char>() + off * 4, b->st[b->cur][k].as<char>() + s->part_off * 4,
+                              (size_t)s->np * 4, cudaMemcpyDeviceToDevice, st),
+              "compact");
+      off += s->np;
+      keep.push_back(std::move(s));
+    }
+  }
+  PB_CK(cudaStreamSynchronize(st), "retire sync");
+  b->sims = std::move(keep);
+  b->cur = dst;
+  b->dirty = true;
+  b->keys_valid = false;
+  return PM_OK;
+}
+
+SimRec* find_sim(pm_batch* b, int id) {
+  for (auto& s : b->sims)
+    if (s->id == id) return s.get();
+  for (auto& s : b->retired)
+    if (s->id == id) return s.get();
+  return nullptr;
+}
+
+int read_back_a(pm_batch* b, cudaStream_t st) {
+  // host mirrors of a / step are advanced in run_steps; nothing to read
+  (void)b;
+  (void)st;
+  return PM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t pm_sim_footprint(const pm_config* cfg) { return cfg ? footprint(*cfg) : 0; }
+
+int pm_batch_create(int device, size_t mem_cap_bytes, pm_batch** out) {
+  if (!out) return PM_ERR_ARG;
+  *out = nullptr;
+  pm_batch* b = new pm_batch();
+  b->device = device;
+  b->cap = mem_cap_bytes;
+  cudaError_t e = cudaSetDevice(device);
+  if (!e) b->sms = sm_count(device);
+  if (!e) e = b->d_err.ensure(sizeof(int));
+  if (!e) e = cudaMemset(b->d_err.p, 0, sizeof(int));
+  if (!e) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
+  if (!e) e = cudaDeviceSynchronize();
+  if (e) {
+    pm_batch_destroy(b);
+    return e == cudaErrorMemoryAllocation ? PM_ERR_OOM : PM_ERR_CUDA;
+  }
+  *out = b;
+  return PM_OK;
+}
+
+void pm_batch_destroy(pm_batch* b) {
+  if (!b) return;
+  drop_graphs(b);
+  for (int w = 0; w < 2; ++w)
+    for (int k = 0; k < kStateArrays; ++k) b->st[w][k].release();
+  for (auto& s : b->sims) {
+    s->grid.release(); s->spec.release(); s->rho.release(); s->fin_pos.release(); s->fin_vel.release();
+  }
+  for (auto& s : b->retired) {
+    s->fin_pos.release(); s->fin_vel.release();
+  }
+  for (auto& t : b->tables) t.second->release();
+  for (auto& l : b->lattices) l.second->release();
+  b->sort.release();
+  b->row_start.release();
+  b->d_sims.release();
+  b->d_prefix.release();
+  b->d_err.release();
+  if (b->own) cudaStreamDestroy(b->own);
+  delete b;
+}
+
+const char* pm_batch_last_error(const pm_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int pm_batch_set_graphs(pm_batch* b, int enable) {
+  if (!b) return PM_ERR_ARG;
+  b->graphs = enable != 0;
+  drop_graphs(b);
+  return PM_OK;
+}
+
+int pm_batch_add(pm_batch* b, const pm_config* cfg, const float* positions, const float* velocities,
+                 int on_device, int* sim_id) {
+  if (!b) return PM_ERR_ARG;
+  if (!cfg || !positions || !velocities || !sim_id) return bfail(b, PM_ERR_ARG, "null argument");
+  if (!grid_supported(cfg->n_cells)) return bfail(b, PM_ERR_ARG, "unsupported N_CELLS");
+  if (cfg->n_parts <= 0 || cfg->n_parts > 1024) return bfail(b, PM_ERR_ARG, "unsupported N_PARTS");
+  if (cfg->steps <= 0 || !(cfg->a_init > 0.0) || !(cfg->a_end > cfg->a_init))
+    return bfail(b, PM_ERR_ARG, "bad time range");
+  const size_t need = footprint(*cfg);
+  if (b->cap && used_bytes(b) + need > b->cap) return bfail(b, PM_ERR_ADMIT, "memory cap reached");
+  cudaStream_t st = nullptr;
+  std::unique_ptr<SimRec> r(new SimRec());
+  r->id = b->next_id++;
+  r->cfg = *cfg;
+  r->n = cfg->n_cells;
+  r->np1 = cfg->n_parts;
+  r->np = (long long)cfg->n_parts * cfg->n_parts * cfg->n_parts;
+  r->da = (cfg->a_end - cfg->a_init) / cfg->steps;
+  r->a = cfg->a_init;
+  {  // pmesh.py:56,63 loop count
+    double a = cfg->a_init;
+    int k = 0;
+    while (a < cfg->a_end - r->da) { a += r->da; ++k; }
+    r->nsteps = k;
+  }
+  const size_t gb = (size_t)r->n * r->n * r->n * sizeof(float);
+  PB_CK(r->grid.ensure(gb), "alloc grid");
+  if (cfg->flags & PM_FLAG_KEEP_DENSITY) PB_CK(r->rho.ensure(gb), "alloc density");
+  PB_CK(r->spec.ensure((size_t)r->n * r->n * spec_pitch(r->n) * sizeof(float2)), "alloc spectrum");
+  PB_CK(tables_for(b, r->n)->build(r->n), "tables");
+  Lattice* l = lattice_for(b, r->np1, r->n);
+  PB_CK(l->build(r->np1, r->n), "lattice");
+  const long long off = resident_particles(b);
+  PB_CK(grow_state(b, off + r->np, st), "alloc state");
+  const float* dp = positions;
+  const float* dv = velocities;
+  DBuf tp, tv;
+  const size_t pb = (size_t)3 * r->np * sizeof(float);
+  if (!on_device) {
+    PB_CK(tp.ensure(pb), "alloc staging");
+    PB_CK(tv.ensure(pb), "alloc staging");
+    PB_CK(cudaMemcpy(tp.p, positions, pb, cudaMemcpyHostToDevice), "h2d");
+    PB_CK(cudaMemcpy(tv.p, velocities, pb, cudaMemcpyHostToDevice), "h2d");
+    dp = tp.as<float>();
+    dv = tv.as<float>();
+  }
+  PB_CK(launch_abs_to_disp(dp, dv, r->np, r->np1, r->n, l->qi.as<int>(), l->qf.as<float>(), state(b, b->cur), off,
+                           st),
+        "convert");
+  PB_CK(cudaStreamSynchronize(st), "sync");
+  tp.release();
+  tv.release();
+  r->part_off = off;
+  r->resident = true;
+  *sim_id = r->id;
+  b->sims.push_back(std::move(r));
+  b->dirty = true;
+  b->keys_valid = false;
+  return PM_OK;
+}
+
+int pm_batch_step(pm_batch* b, int nsteps, void* stream) {
+  if (!b) return PM_ERR_ARG;
+  if (nsteps < 0) return bfail(b, PM_ERR_ARG, "negative step count");
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->own;
+  if (!stream) PB_CK(cudaDeviceSynchronize(), "sync");  // order after legacy-stream work
+  int left = nsteps;
+  while (left > 0 && !b->sims.empty()) {
+    if (int r = retire_finished(b, st)) return r;
+    if (b->sims.empty()) break;
+    if (b->dirty) {
+      if (int r = build_plan(b, st)) return r;
+    }
+    int k = left;
+    for (auto& s : b->sims) k = std::min(k, s->nsteps - s->done);
+    if (k <= 0) break;
+    if (int r = ensure_keys(b, st)) return r;
+    if (int r = run_steps(b, k, st)) return r;
+    for (auto& s : b->sims) {
+      for (int i = 0; i < k; ++i) s->a += s->da;
+      s->done += k;
+    }
+    left -= k;
+  }
+  const int r = retire_finished(b, st);
+  if (!stream && r == PM_OK) PB_CK(cudaStreamSynchronize(st), "sync");
+  return r;
+}
+
+int pm_batch_active(pm_batch* b, int sim_id) {
+  if (!b) return -1;
+  for (auto& s : b->sims)
+    if (s->id == sim_id) return s->done < s->nsteps ? 1 : 0;
+  for (auto& s : b->retired)
+    if (s->id == sim_id) return 0;
+  return -1;
+}
+
+int pm_batch_get(pm_batch* b, int sim_id, float* positions, float* velocities, int to_device, double* a,
+                 int* steps_done, void* stream) {
+  if (!b) return PM_ERR_ARG;
+  SimRec* s = find_sim(b, sim_id);
+  if (!s) return bfail(b, PM_ERR_ARG, "unknown simulation id");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (a) *a = s->a;
+  if (steps_done) *steps_done = s->done;
+  if (!positions && !velocities) return PM_OK;
+  const size_t pb = (size_t)3 * s->np * sizeof(float);
+  const float* sp;
+  const float* sv;
+  DBuf tp, tv;
+  if (s->resident) {
+    PB_CK(tp.ensure(pb), "alloc staging");
+    PB_CK(tv.ensure(pb), "alloc staging");
+    Lattice* l = lattice_for(b, s->np1, s->n);
+    PB_CK(launch_disp_to_abs(state(b, b->cur), s->part_off, s->np, s->np1, s->n, l->qi.as<int>(),
+                             l->qf.as<float>(), tp.as<float>(), tv.as<float>(), st),
+          "extract");
+    sp = tp.as<float>();
+    sv = tv.as<float>();
+  } else {
+    sp = s->fin_pos.as<float>();
+    sv = s->fin_vel.as<float>();
+  }
+  const cudaMemcpyKind kind = to_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (positions) PB_CK(cudaMemcpyAsync(positions, sp, pb, kind, st), "copy out");
+  if (velocities) PB_CK(cudaMemcpyAsync(velocities, sv, pb, kind, st), "copy out");
+  PB_CK(cudaStreamSynchronize(st), "sync");
+  tp.release();
+  tv.release();
+  return read_back_a(b, st);
+}
+
+int pm_batch_remove(pm_batch* b, int sim_id) {
+  if (!b) return PM_ERR_ARG;
+  for (size_t i = 0; i < b->retired.size(); ++i) {
+    if (b->retired[i]->id == sim_id) {
+      b->retired[i]->fin_pos.release();
+      b->retired[i]->fin_vel.release();
+      b->retired.erase(b->retired.begin() + i);
+      return PM_OK;
+    }
+  }
+  for (auto& s : b->sims) {
+    if (s->id == sim_id) {
+      s->done = s->nsteps;  // retire now, then drop
+      cudaStream_t st = nullptr;
+      if (int r = retire_finished(b, st)) return r;
+      return pm_batch_remove(b, sim_id);
+    }
+  }
+  return bfail(b, PM_ERR_ARG, "unknown simulation id");
+}
+
+int pm_batch_check(pm_batch* b, void* stream, int* bits) {
+  if (!b || !bits) return PM_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  int h = 0;
+  PB_CK(cudaMemcpyAsync(&h, b->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "read flags");
+  PB_CK(cudaMemsetAsync(b->d_err.p, 0, sizeof(int), st), "clear flags");
+  PB_CK(cudaStreamSynchronize(st), "sync");
+  *bits = h;
+  return h ? bfail(b, PM_ERR_DEVICE, "device check bits " + std::to_string(h)) : PM_OK;
+}
+
+}  // extern "C"

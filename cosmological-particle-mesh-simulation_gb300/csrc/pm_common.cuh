@@ -1,0 +1,139 @@
+// Shared device/host declarations of the GB300 particle-mesh engine.
+//
+// Data layout in HBM (one simulation):
+//   real grids (density, potential)  float  [z][y][x], n^3
+//   half spectrum                    float2 [z][y][kx], kx in [0, n/2], row pitch `pitch`
+//                                    (a multiple of 16 complex = 128 B)
+//   particles                        structure of arrays, one float per axis and
+//                                    per quantity (the reference's (3, Np) layout)
+// Many simulations share one launch per phase: every kernel receives the device
+// array of `Sim` descriptors and a per-phase work prefix (CTA -> simulation).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define PM_FIX_BITS 26          // CIC weights are accumulated as integers w * 2^26
+#define PM_MAX_N 1024
+
+namespace pm {
+
+enum : int {
+  ERR_OK = 0,
+  ERR_CELL_RANGE = 1,   // a particle cell fell outside the grid (NaN/Inf position)
+  ERR_SOURCE_ROW = 2,   // deposit: particle outside the tile's source rows (sort broken)
+  ERR_NONFINITE = 4,    // kick/drift produced a non-finite coordinate
+};
+
+enum PosMode : int { POS_ABS = 0, POS_DISP = 1 };
+
+// Device-side description of one simulation.  All pointers are device pointers.
+struct Sim {
+  int n;            // grid cells per side
+  int pitch;        // spectrum row pitch in complex elements
+  int np1;          // particles per side of the Lagrangian lattice (0: unknown)
+  int xbits;        // bits of x in the cell key
+  int ty, tz;       // deposit tile: tz planes x ty rows of full x-rows
+  int flags;
+  int pad0;
+  long long np;        // particle count
+  long long part_off;  // first particle slot in the batch particle arrays
+  unsigned row_base;   // first global row number of this simulation
+  unsigned pad1;
+  float* rho;          // density n^3 (output of the deposit)
+  float2* spec;        // half spectrum
+  float* phi;          // potential n^3
+  const float* fgrid;  // optional caller Green table n^3 (nullptr: computed in-kernel)
+  const float* s2;     // sin^2(pi m / n), m < n
+  const float2* tw;    // exp(-2 pi i m / n), m < n
+  const int* q_int;    // lattice coordinate, integer part, np1 entries
+  const float* q_frac; // lattice coordinate, fractional part, np1 entries
+  // per-step coefficients
+  float mass_scale;    // particle mass * 2^-PM_FIX_BITS
+  float green;         // -3 Om / (8 a) / n^3
+  float kick;          // da * f(a + da)
+  float drift;         // da * f(a + da) / (a + da)^2
+  // time state (fp64, advanced on the device in resident mode)
+  double a, da, om, ol, ok, h0;
+  int step, nsteps, active, fix_f;
+};
+
+// CTA -> simulation map of one phase: prefix[s] = first work unit of simulation s.
+struct Work {
+  const int* prefix;  // nsims + 1 entries (device)
+  int nsims;
+  int total;          // prefix[nsims]
+};
+
+// Particle arrays of a batch (structure of arrays, indexed by slot).
+struct Parts {
+  float* x; float* y; float* z;       // positions (POS_ABS) or displacements (POS_DISP)
+  float* vx; float* vy; float* vz;
+  unsigned* id;                        // Lagrangian particle index (POS_DISP)
+};
+
+__device__ __forceinline__ int locate_sim(const Work& w, int unit) {
+  int lo = 0, hi = w.nsims - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&w.prefix[mid]) <= unit) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void set_error(int* err, int code) {
+  if (err) atomicOr(err, code);
+}
+
+// ---------------------------------------------------------------------------------
+// Launchers (defined in the .cu files, called by the engine)
+// ---------------------------------------------------------------------------------
+// spectral passes: one kernel per grid size n (supported n: spectral_supported)
+enum SpecKind : int { SPEC_X_R2C = 0, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Z_TABLE, SPEC_Y_INV, SPEC_X_C2R,
+                      SPEC_PREPARE /* only set kernel attributes */ };
+template <int N>
+cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cudaStream_t st);
+bool spectral_supported(int n);
+// work units (CTAs' worth of work) of one spectral pass for a grid of size n
+long long spectral_units(SpecKind kind, int n);
+// resident CTAs per SM of a spectral pass for size n (for persistent grid sizing)
+int spectral_ctas_per_sm(SpecKind kind, int n);
+cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int ctas, cudaStream_t st);
+cudaError_t launch_fourier_grid(const Sim* sims, int ctas, cudaStream_t st);
+
+// particle kernels
+cudaError_t launch_keys_abs(const Sim* sims, const Work& w, Parts p, unsigned* keys, unsigned* vals,
+                            int* err, int ctas, cudaStream_t st);
+cudaError_t launch_keys_disp(const Sim* sims, const Work& w, Parts p, unsigned* keys, unsigned* vals,
+                             int* err, int ctas, cudaStream_t st);
+cudaError_t launch_row_start(const unsigned* keys, long long n, int xbits, unsigned nrows,
+                             unsigned* row_start, cudaStream_t st);
+cudaError_t launch_deposit(const Sim* sims, const Work& w, Parts p, const unsigned* perm,
+                           const unsigned* row_start, int mode, int* err, int ctas, size_t smem,
+                           cudaStream_t st);
+cudaError_t launch_kick(const Sim* sims, const Work& w, Parts in, Parts out, const unsigned* perm,
+                        unsigned* keys_next, int mode, int* err, int ctas, cudaStream_t st);
+cudaError_t launch_coef(Sim* sims, int nsims, int advance, cudaStream_t st);
+cudaError_t deposit_prepare();  // sets kernel attributes (call before graph capture)
+cudaError_t launch_abs_to_disp(const float* pos, const float* vel, long long np, int np1, int n,
+                               const int* q_int, const float* q_frac, Parts out, long long off,
+                               cudaStream_t st);
+cudaError_t launch_disp_to_abs(Parts in, long long off, long long np, int np1, int n, const int* q_int,
+                               const float* q_frac, float* pos, float* vel, cudaStream_t st);
+size_t deposit_smem_bytes(int n, int ty, int tz);
+
+// radix sort of (key, value) pairs, stable, LSD, 8-bit digits
+struct SortScratch {
+  unsigned* keys_alt; unsigned* vals_alt;
+  unsigned* hist;     // 256 * max_blocks
+  unsigned* digit_tot;
+  long long capacity; int max_blocks;
+};
+constexpr int SORT_TILE = 4096;
+size_t sort_scratch_hist_entries(long long n);
+// Sorts keys[0,n) / vals[0,n) on bits [0, bits).  Returns via *in_alt whether the result
+// sits in the scratch (alt) buffers.  When gen_vals is set, vals are not read on the
+// first pass and the identity 0..n-1 is used instead.
+cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int bits, bool gen_vals,
+                       const SortScratch& s, bool* in_alt, cudaStream_t st);
+
+}  // namespace pm

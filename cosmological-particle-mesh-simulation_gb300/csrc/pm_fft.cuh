@@ -1,0 +1,170 @@
+// Shared-memory Stockham FFT for batches of lines (radix 2, 3, 4, 8).
+//
+// A CTA holds NL lines of L complex elements in shared memory, element j of line l at
+// s[j * LS + l] (lines interleaved, so consecutive threads touch consecutive words).
+// Each pass loads all of its butterflies into registers, synchronises, and writes the
+// self-sorted (Stockham) output back in place; the last pass leaves natural order.
+// Twiddles come from a table tw[m] = exp(-2 pi i m / (L * tws)) read with stride tws.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace pm {
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// multiply by -i (forward transform) or +i (inverse transform)
+template <bool INV>
+__device__ __forceinline__ float2 mul_mi(float2 a) {
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// ---------------------------------------------------------------------------------
+// Small DFTs in registers.  Forward uses exp(-2 pi i jk / R), inverse exp(+...).
+// ---------------------------------------------------------------------------------
+template <int R, bool INV> struct DFT;
+
+template <bool INV> struct DFT<2, INV> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float2 a = v[0];
+    v[0] = cadd(a, v[1]);
+    v[1] = csub(a, v[1]);
+  }
+};
+
+template <bool INV> struct DFT<4, INV> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+    const float2 t2 = cadd(v[1], v[3]), t3 = mul_mi<INV>(csub(v[1], v[3]));
+    v[0] = cadd(t0, t2);
+    v[2] = csub(t0, t2);
+    v[1] = cadd(t1, t3);
+    v[3] = csub(t1, t3);
+  }
+};
+
+template <bool INV> struct DFT<3, INV> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float s3 = 0.866025403784438646763723f;  // sin(2 pi / 3)
+    const float2 s = cadd(v[1], v[2]);
+    const float2 d = csub(v[1], v[2]);
+    const float2 m = make_float2(v[0].x - 0.5f * s.x, v[0].y - 0.5f * s.y);
+    const float2 t = cscale(mul_mi<INV>(d), s3);
+    v[0] = cadd(v[0], s);
+    v[1] = cadd(m, t);
+    v[2] = csub(m, t);
+  }
+};
+
+template <bool INV> struct DFT<8, INV> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float c = 0.707106781186547524400844f;  // sqrt(1/2)
+    float2 e[4] = {v[0], v[2], v[4], v[6]};
+    float2 o[4] = {v[1], v[3], v[5], v[7]};
+    DFT<4, INV>::run(e);
+    DFT<4, INV>::run(o);
+    // o[k] *= exp(-/+ 2 pi i k / 8)
+    const float2 o1 = o[1], o3 = o[3];
+    if (!INV) {
+      o[1] = make_float2(c * (o1.x + o1.y), c * (o1.y - o1.x));
+      o[3] = make_float2(c * (o3.y - o3.x), -c * (o3.x + o3.y));
+    } else {
+      o[1] = make_float2(c * (o1.x - o1.y), c * (o1.x + o1.y));
+      o[3] = make_float2(-c * (o3.x + o3.y), c * (o3.x - o3.y));
+    }
+    o[2] = mul_mi<INV>(o[2]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      v[k] = cadd(e[k], o[k]);
+      v[k + 4] = csub(e[k], o[k]);
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------------
+// Radix plans (product of radices == L)
+// ---------------------------------------------------------------------------------
+template <int L> struct Plan;
+#define PM_PLAN(L_, ...)                                   \
+  template <> struct Plan<L_> {                            \
+    static constexpr int r[] = {__VA_ARGS__};              \
+    static constexpr int np = sizeof(r) / sizeof(int);     \
+  };
+PM_PLAN(8, 8)
+PM_PLAN(12, 3, 4)
+PM_PLAN(16, 4, 4)
+PM_PLAN(24, 3, 8)
+PM_PLAN(32, 4, 8)
+PM_PLAN(48, 3, 4, 4)
+PM_PLAN(64, 8, 8)
+PM_PLAN(96, 3, 4, 8)
+PM_PLAN(128, 2, 8, 8)
+PM_PLAN(192, 3, 8, 8)
+PM_PLAN(256, 4, 8, 8)
+PM_PLAN(384, 3, 2, 8, 8)
+PM_PLAN(512, 8, 8, 8)
+PM_PLAN(768, 3, 4, 8, 8)
+PM_PLAN(1024, 2, 8, 8, 8)
+#undef PM_PLAN
+
+// One Stockham pass of radix R on NL lines (in place through registers).
+template <int L, int R, int NS, int NL, int LS, int NT, bool INV>
+__device__ __forceinline__ void stockham_pass(float2* s, const float2* __restrict__ tw, int tws) {
+  constexpr int NB = L / R;
+  constexpr int NTASK = NL * NB;
+  constexpr int TPT = (NTASK + NT - 1) / NT;
+  float2 v[TPT][R];
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    const int task = threadIdx.x + t * NT;
+    if ((NTASK % NT) == 0 || task < NTASK) {
+      const int line = task % NL, j = task / NL;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[t][r] = s[(j + r * NB) * LS + line];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    const int task = threadIdx.x + t * NT;
+    if ((NTASK % NT) == 0 || task < NTASK) {
+      const int line = task % NL, j = task / NL;
+      const int k = j % NS;
+      if (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          float2 w = __ldg(&tw[(r * k * (L / (NS * R))) * tws]);
+          if (INV) w.y = -w.y;
+          v[t][r] = cmul(v[t][r], w);
+        }
+      }
+      DFT<R, INV>::run(v[t]);
+      const int base = (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) s[(base + r * NS) * LS + line] = v[t][r];
+    }
+  }
+  __syncthreads();
+}
+
+template <int L, int P, int NS, int NL, int LS, int NT, bool INV>
+__device__ __forceinline__ void fft_passes(float2* s, const float2* __restrict__ tw, int tws) {
+  if constexpr (P < Plan<L>::np) {
+    constexpr int R = Plan<L>::r[P];
+    stockham_pass<L, R, NS, NL, LS, NT, INV>(s, tw, tws);
+    fft_passes<L, P + 1, NS * R, NL, LS, NT, INV>(s, tw, tws);
+  }
+}
+
+// Unnormalised DFT of NL interleaved lines of length L held in shared memory.
+// Must be entered by all NT threads after a __syncthreads(); returns synchronised.
+template <int L, int NL, int LS, int NT, bool INV>
+__device__ __forceinline__ void fft_lines(float2* s, const float2* __restrict__ tw, int tws) {
+  fft_passes<L, 0, 1, NL, LS, NT, INV>(s, tw, tws);
+}
+
+}  // namespace pm

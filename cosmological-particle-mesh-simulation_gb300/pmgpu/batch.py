@@ -1,0 +1,113 @@
+"""Resident batch engine: many simulations advancing together on one GPU."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .config import Config
+
+
+class Batch:
+    """Wraps pm_batch_*.  Simulations are admitted from absolute (3, N_PARTS^3) float32
+    positions / velocities (numpy on the host or CUDA tensors) and advance together."""
+
+    def __init__(self, device: int = 0, mem_cap_bytes: int = 0, graphs: bool = True):
+        self._lib = _lib.load()
+        self.device = device
+        torch.cuda.init()
+        h = ctypes.c_void_p()
+        with torch.cuda.device(device):
+            rc = self._lib.pm_batch_create(device, int(mem_cap_bytes), ctypes.byref(h))
+        if rc != 0:
+            raise _lib.PMError(rc, "pm_batch_create failed")
+        self._h = h
+        self.cfgs: dict[int, Config] = {}
+        if not graphs:
+            self._lib.pm_batch_set_graphs(self._h, 0)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.pm_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise _lib.PMError(rc, self._lib.pm_batch_last_error(self._h).decode(errors="replace"))
+
+    @staticmethod
+    def footprint(cfg: Config) -> int:
+        return int(_lib.load().pm_sim_footprint(ctypes.byref(cfg.c_struct())))
+
+    def add(self, cfg: Config, positions, velocities) -> int:
+        on_dev = isinstance(positions, torch.Tensor) and positions.is_cuda
+        if on_dev:
+            positions = positions.contiguous()
+            velocities = velocities.contiguous()
+            pp, vp = positions.data_ptr(), velocities.data_ptr()
+        else:
+            positions = np.ascontiguousarray(positions, dtype=np.float32)
+            velocities = np.ascontiguousarray(velocities, dtype=np.float32)
+            pp, vp = positions.ctypes.data, velocities.ctypes.data
+        sid = ctypes.c_int(0)
+        self._check(self._lib.pm_batch_add(self._h, ctypes.byref(cfg.c_struct()), ctypes.c_void_p(pp),
+                                           ctypes.c_void_p(vp), 1 if on_dev else 0, ctypes.byref(sid)))
+        self.cfgs[sid.value] = cfg
+        return sid.value
+
+    def step(self, nsteps: int = 1):
+        stream = torch.cuda.current_stream().cuda_stream
+        self._check(self._lib.pm_batch_step(self._h, int(nsteps), ctypes.c_void_p(stream)))
+
+    def active(self, sid: int) -> bool:
+        r = self._lib.pm_batch_active(self._h, sid)
+        if r < 0:
+            raise KeyError(sid)
+        return r == 1
+
+    def get(self, sid: int, device: bool = False):
+        cfg = self.cfgs[sid]
+        npart = cfg.np_total
+        a = ctypes.c_double(0)
+        done = ctypes.c_int(0)
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        if device:
+            pos = torch.empty((3, npart), dtype=torch.float32, device=f"cuda:{self.device}")
+            vel = torch.empty_like(pos)
+            self._check(self._lib.pm_batch_get(self._h, sid, ctypes.c_void_p(pos.data_ptr()),
+                                               ctypes.c_void_p(vel.data_ptr()), 1, ctypes.byref(a),
+                                               ctypes.byref(done), stream))
+        else:
+            pos = np.empty((3, npart), dtype=np.float32)
+            vel = np.empty_like(pos)
+            self._check(self._lib.pm_batch_get(self._h, sid, ctypes.c_void_p(pos.ctypes.data),
+                                               ctypes.c_void_p(vel.ctypes.data), 0, ctypes.byref(a),
+                                               ctypes.byref(done), stream))
+        return pos, vel, a.value, done.value
+
+    def state(self, sid: int):
+        a = ctypes.c_double(0)
+        done = ctypes.c_int(0)
+        self._check(self._lib.pm_batch_get(self._h, sid, None, None, 0, ctypes.byref(a), ctypes.byref(done),
+                                           None))
+        return a.value, done.value
+
+    def remove(self, sid: int):
+        self._check(self._lib.pm_batch_remove(self._h, sid))
+        self.cfgs.pop(sid, None)
+
+    def check_device(self):
+        bits = ctypes.c_int(0)
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        rc = self._lib.pm_batch_check(self._h, stream, ctypes.byref(bits))
+        if rc != 0:
+            what = [v for k, v in _lib.DEVICE_BITS.items() if bits.value & k]
+            raise _lib.PMError(rc, "device check failed: " + "; ".join(what))

@@ -1,0 +1,143 @@
+/*
+ * pm_gb300.h -- C ABI of the GB300 particle-mesh engine (libpm_gb300.so).
+ *
+ * The drop-in entry points replace, one for one, the functions of the per-step hot
+ * path of grkooij/Cosmological-Particle-Mesh-Simulation (citations are path:line in
+ * that project).  Sizes and cosmology come from a pm_config that mirrors
+ * src/configure_me.py.  Arrays follow the reference's layouts:
+ *
+ *   positions, velocities   float32, (3, np) row-major: x[np], then y[np], then z[np]
+ *   density, potential,     float32, (N, N, N) indexed [z][y][x]
+ *   fourier grid
+ *
+ * All array arguments are DEVICE pointers unless the name says host; `stream` is a
+ * cudaStream_t (NULL = legacy default stream).  Every call returns PM_OK or a
+ * nonzero status; pm_last_error() returns the message of the last failure.  The
+ * caller owns all arrays it passes; a context owns its scratch memory and tables.
+ * Contexts are not thread-safe: use one per host thread.
+ */
+#ifndef PM_GB300_H
+#define PM_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PM_OK 0
+#define PM_ERR_ARG 1      /* invalid argument or unsupported size */
+#define PM_ERR_CUDA 2     /* CUDA runtime error */
+#define PM_ERR_OOM 3      /* device allocation failed */
+#define PM_ERR_DEVICE 4   /* device-side check failed (see pm_check_device) */
+#define PM_ERR_ADMIT 5    /* batch admission refused: memory cap */
+
+/* device check bits reported by pm_check_device */
+#define PM_DEV_CELL_RANGE 1  /* a particle coordinate was not finite / off grid */
+#define PM_DEV_SOURCE_ROW 2  /* deposit found a particle outside its tile (unsorted input) */
+#define PM_DEV_NONFINITE 4   /* kick/drift produced a non-finite value */
+
+/* flags of pm_config */
+#define PM_FLAG_FIX_COSMO_F 1  /* f(a) with Omega_m in its slot; the reference passes H0
+                                  there (src/integrate.py:12) and is followed by default */
+#define PM_FLAG_KEEP_DENSITY 2 /* batch: keep the density grid apart from the potential */
+
+/* Mirrors src/configure_me.py:7-40 (plotting / saving switches omitted). */
+typedef struct pm_config {
+  int n_cells;          /* N_CELLS, grid cells per side (configure_me.py:8) */
+  int n_parts;          /* N_PARTS, particles per side (configure_me.py:7) */
+  double box_size;      /* BOX_SIZE in Mpc/h (configure_me.py:9) */
+  double omega_m0;      /* OMEGA_M0 (configure_me.py:34) */
+  double omega_b0;      /* OMEGA_B0 (configure_me.py:35) */
+  double omega_k0;      /* OMEGA_K0 (configure_me.py:36) */
+  double omega_lambda0; /* OMEGA_LAMBDA0 (configure_me.py:37) */
+  double h0;            /* H0 (configure_me.py:38) */
+  double a_init;        /* A_INIT (configure_me.py:39) */
+  double a_end;         /* A_END (configure_me.py:40) */
+  int steps;            /* STEPS (configure_me.py:14) */
+  int flags;            /* PM_FLAG_* */
+} pm_config;
+
+typedef struct pm_ctx pm_ctx;
+
+/* ---- context ------------------------------------------------------------------- */
+int pm_ctx_create(const pm_config* cfg, int device, pm_ctx** out);
+void pm_ctx_destroy(pm_ctx* ctx);
+const char* pm_last_error(const pm_ctx* ctx);
+/* Synchronises `stream`, returns (and clears) the device check bits in *bits. */
+int pm_check_device(pm_ctx* ctx, void* stream, int* bits);
+/* Grid sizes the kernels support (N = 2^a 3^b, 16 <= N <= 1024, N % 8 == 0 or N = 24). */
+int pm_supported_n(int n);
+
+/* ---- drop-in hot path ----------------------------------------------------------- */
+/* src/density.py:7-48  density(positions, mass) -> grid.
+   Deterministic: cell-key radix sort + tiled integer-accumulated CIC deposit. */
+int pm_density(pm_ctx* ctx, const float* positions, long long np, double mass, float* rho,
+               void* stream);
+
+/* src/fourier_utils.py:5-16  fourier_grid() -> 1/sum(sin^2(k/2)), k=0 entry 0. */
+int pm_fourier_grid(pm_ctx* ctx, float* fgrid, void* stream);
+
+/* src/potential.py:7-29  potential(density, fgrid, a) -> phi.
+   fgrid == NULL evaluates the reference Green function in-kernel (no table read). */
+int pm_potential(pm_ctx* ctx, const float* rho, const float* fgrid, double a, float* phi,
+                 void* stream);
+
+/* src/integrate.py:15-97  integrate(positions, velocities, a_val, f_a1, da, potentials);
+   positions and velocities are updated in place. */
+int pm_integrate(pm_ctx* ctx, float* positions, float* velocities, long long np, double a,
+                 double f_a1, double da, const float* phi, void* stream);
+
+/* src/integrate.py:9-13  advance_time(density, positions, velocities, fgrid, a, da);
+   positions and velocities are updated in place. */
+int pm_advance_time(pm_ctx* ctx, const float* rho, float* positions, float* velocities,
+                    long long np, const float* fgrid, double a, double da, void* stream);
+
+/* src/pmesh.py:60-61  loop body: rho = density(positions, mass);
+   advance_time(rho, positions, velocities, fgrid, a, da).  rho_out may be NULL. */
+int pm_step(pm_ctx* ctx, float* positions, float* velocities, long long np, double mass,
+            double a, double da, float* rho_out, void* stream);
+
+/* Same as pm_step on HOST arrays (pinned for full speed): copies in, steps, copies out. */
+int pm_step_host(pm_ctx* ctx, float* h_positions, float* h_velocities, long long np,
+                 double mass, double a, double da, void* stream);
+
+/* src/cosmology.py:20-27  f(a, [om, ol, ok]). */
+double pm_cosmo_f(double a, double om, double ol, double ok);
+
+/* Cell keys of the deposit ordering and their stable sort (bit-exact integer work):
+   keys_out[i] = key of particle i; sorted_keys / perm = the sorted keys and the
+   particle index of each sorted entry.  Any output may be NULL. */
+int pm_sort_keys(pm_ctx* ctx, const float* positions, long long np, unsigned* keys_out,
+                 unsigned* sorted_keys, unsigned* perm, void* stream);
+
+/* ---- resident engine: batches of simulations ------------------------------------ */
+typedef struct pm_batch pm_batch;
+
+/* mem_cap_bytes = 0: no cap.  Simulations advance together, one launch per phase. */
+int pm_batch_create(int device, size_t mem_cap_bytes, pm_batch** out);
+void pm_batch_destroy(pm_batch* b);
+const char* pm_batch_last_error(const pm_batch* b);
+/* Device bytes a simulation of this configuration holds while resident. */
+size_t pm_sim_footprint(const pm_config* cfg);
+/* Admits a simulation from absolute positions/velocities (3, N_PARTS^3) at cfg->a_init;
+   on_device selects device or host input arrays.  PM_ERR_ADMIT if over the cap. */
+int pm_batch_add(pm_batch* b, const pm_config* cfg, const float* positions,
+                 const float* velocities, int on_device, int* sim_id);
+/* Advances every active simulation by up to nsteps steps (a simulation stops after the
+   src/pmesh.py:56 loop count).  Work is enqueued on `stream` (CUDA graphs). */
+int pm_batch_step(pm_batch* b, int nsteps, void* stream);
+/* Copies a simulation's state out (absolute positions in particle order). */
+int pm_batch_get(pm_batch* b, int sim_id, float* positions, float* velocities, int to_device,
+                 double* a, int* steps_done, void* stream);
+/* 1 while the simulation still has steps to run, 0 when done, <0 if unknown id. */
+int pm_batch_active(pm_batch* b, int sim_id);
+int pm_batch_remove(pm_batch* b, int sim_id);
+int pm_batch_set_graphs(pm_batch* b, int enable);
+/* Device check bits of the batch (synchronises). */
+int pm_batch_check(pm_batch* b, void* stream, int* bits);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PM_GB300_H */
