@@ -1,0 +1,359 @@
+"""Benchmark of the GB300 particle-mesh engine on the README workload.
+
+Workload (one "step" = one PM step of the hot path): 256^3 particles on a 512^3 grid,
+box 250 Mpc/h, LCDM (Om 0.3, OL 0.7, h 0.7, ns 0.96, reference normalisation), seeded
+GRF + Zel'dovich ICs at a = 0.02, leapfrog with da = 0.98/1000 (1000 STEPS).  The timed
+steps are the first K steps of that run.
+
+  value   resident engine (pm_batch_*): state in HBM, K steps timed with CUDA events
+          (graph replays), particle-updates/s = 256^3 * K / time.
+  e2e     the drop-in loop through the C ABI on HOST arrays (pm_step_host): every step
+          copies positions+velocities in from pinned host memory and back out.
+  roofline  the phase with the largest share of the step, from CUDA events recorded on
+          the launch stream around each phase (pm_batch_profile), against its
+          algorithmic bytes.
+  cpu_baseline  the FP64 numpy/scipy port of the reference path (oracle/) on the host
+          cores, one bounded sample of full-size steps.
+
+``--impl reference`` times only that CPU port (the reference itself needs numba and
+pyFFTW, which are not installed) and prints its own line.  With torchrun and N > 1 each
+rank runs an independent replica ("replicas only": one simulation does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cosmological-particle-mesh-simulation_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "particle-updates/s (plain vs batched/served) at P(k)≤0.5% err; p50/p99 sim latency"
+UNIT = "particle-updates/s"
+WORKLOAD = ("README workload: 256^3 particles, 512^3 grid, box 250 Mpc/h, LCDM, seeded GRF + "
+            "Zel'dovich ICs at a=0.02, 1000 leapfrog steps to a=1 (first K steps timed)")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload_config(steps_needed: int, n_parts=256, n_cells=512, box=250.0):
+    from pmgpu.config import Config, step_count
+    cfg = Config(n_parts=n_parts, n_cells=n_cells, box_size=box, random_seed=0, steps=1000, power=0.96,
+                 omega_m0=0.3, omega_b0=0.04, omega_k0=0.0, omega_lambda0=0.7, h0=0.7, a_init=0.02, a_end=1.0)
+    if step_count(cfg.a_init, cfg.a_end, cfg.steps) < steps_needed:
+        # keep da, extend the end so that the driver loop runs at least steps_needed steps
+        cfg.a_end = cfg.a_init + (steps_needed + 2) * cfg.da
+        cfg.steps = steps_needed + 2
+    return cfg
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes (dram__bytes_read.sum + write.sum) of each phase's kernel from
+    the committed ncu summary, scaled to the full workload there; None if absent."""
+    path = os.path.join(ROOT, "profiles", "traffic_cfg2.md")
+    out = {}
+    try:
+        for line in open(path):
+            if line.startswith("traffic:"):
+                _, k, v = line.split()
+                out[k] = float(v)
+    except OSError:
+        pass
+    return out
+
+
+def algorithmic_bytes(np_, n):
+    """Bytes each phase must move once (inputs read once, outputs written once)."""
+    nc = n ** 3
+    h = n * n * (n // 2 + 1)
+    return {
+        "deposit": 12 * np_ + 4 * nc,
+        "x_r2c": 4 * nc + 8 * h,
+        "y_fwd": 16 * h,
+        "z_green": 16 * h,
+        "y_inv": 16 * h,
+        "x_c2r": 8 * h + 4 * nc,
+        "kick": 24 * np_ + 4 * nc + 24 * np_,
+        "sort": 0, "rows": 0, "coef": 0,
+    }
+
+
+def make_ics(cfg):
+    from pmgpu import ics
+    return ics.initial_conditions(cfg)
+
+
+def run_gpu(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    import pmgpu
+    from pmgpu.batch import Batch
+    from pmgpu.context import PMContext
+
+    torch.cuda.set_device(local)
+    pmgpu.build()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    K, W = args.steps, args.warmup
+    cfg = workload_config(max(K, W + args.profile_steps), args.n_parts, args.n_cells, args.box)
+    t0 = time.time()
+    pos, vel = make_ics(cfg)
+    t_ics = time.time() - t0
+    np_ = cfg.np_total
+
+    # ---- warm-up on a throwaway batch (W steps, graphs instantiated), then a per-phase
+    # CUDA-event profile of the next steps of that run ----------------------------------
+    wb = Batch(device=local)
+    wb.add(cfg, pos, vel)
+    wb.step(max(W, 1))
+    prof = wb.profile(args.profile_steps)
+    wb.check_device()
+    wb.close()
+    del wb
+
+    # ---- timed: K steps of a fresh run from the ICs --------------------------------
+    b = Batch(device=local)
+    sid = b.add(cfg, pos, vel)
+    b.step(0)
+    launches = b.launches_per_step()
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk, torch.cuda.stream(stream):
+        ev0.record(stream)
+        b.step(K)  # enqueued on `stream` (graph replays)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    b.check_device()
+    _, done = b.state(sid)
+    if done != K:
+        raise RuntimeError(f"ran {done} steps instead of {K}")
+    b.close()
+
+    t_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = t.item()
+    value = np_ * K * ws / (t_max / 1e3)
+
+    # ---- e2e: drop-in loop on host arrays through the C ABI -------------------------
+    e2e = None
+    if args.e2e_steps > 0:
+        ctx = PMContext(cfg, device=local)
+        hp = torch.from_numpy(pos.copy()).pin_memory()
+        hv = torch.from_numpy(vel.copy()).pin_memory()
+        a = cfg.a_init
+        ctx.step_host(hp, hv, cfg.mass, a, cfg.da)  # warm-up (allocations)
+        hp.copy_(torch.from_numpy(pos))
+        hv.copy_(torch.from_numpy(vel))
+        torch.cuda.synchronize()
+        barrier()
+        te0 = time.perf_counter()
+        for i in range(args.e2e_steps):
+            ctx.step_host(hp, hv, cfg.mass, a, cfg.da)
+            a += cfg.da
+        torch.cuda.synchronize()
+        te = time.perf_counter() - te0
+        ctx.check_device()
+        if dist is not None:
+            t = torch.tensor([te], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te = t.item()
+        e2e = {"value": np_ * args.e2e_steps * ws / te, "unit": UNIT,
+               "h2d_bytes_per_step": 2 * 3 * 4 * np_, "d2h_bytes_per_step": 2 * 3 * 4 * np_,
+               "steps": args.e2e_steps, "api": "pm_step_host (C ABI, pinned host arrays)"}
+        ctx.close()
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant phase --------------------------------------------
+    alg = algorithmic_bytes(np_, cfg.n_cells)
+    dom = max((k for k in prof if alg.get(k, 0) > 0), key=lambda k: prof[k])
+    peak, peak_src = measured_peak()
+    achieved = alg[dom] / (prof[dom] / 1e3) / 1e9
+    traffic = profiled_traffic().get(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                "traffic": traffic, "algorithmic_bytes": alg[dom], "launch_ms": round(prof[dom], 4),
+                "phase_ms": {k: round(v, 4) for k, v in prof.items()},
+                "step_ms_sum_of_phases": round(sum(prof.values()), 4)}
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(cfg, pos, vel, args.cpu_steps)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": t_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: seeded GRF + Zel'dovich ICs (reference algorithm)",
+        "config": {"workload": WORKLOAD if (cfg.n_parts, cfg.n_cells) == (256, 512) else
+                   f"reduced case: {cfg.n_parts}^3 particles, {cfg.n_cells}^3 grid",
+                   "n_parts": cfg.n_parts, "n_cells": cfg.n_cells, "box_size": cfg.box_size, "a_init": 0.02,
+                   "da": cfg.da, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (512^3 grid = 537 MB per field)", "ics_seconds": round(t_ics, 1)},
+        "e2e": e2e, "gpu_launches": launches * K, "roofline": roofline, "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(cfg, pos, vel, steps):
+    """FP64 numpy/scipy port of the reference step (oracle/) on all host cores."""
+    import numpy as np
+    from oracle import pm_oracle as O
+    cores = len(os.sched_getaffinity(0))
+    fg = O.fourier_grid(cfg.n_cells)
+    p, v = pos.astype(np.float32), vel.astype(np.float32)
+    a = cfg.a_init
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        rho = O.density(p, cfg.mass, cfg.n_cells)
+        x, vv = O.advance_time(rho, p, v, fg, a, cfg.da, cfg.omega_m0, cfg.omega_lambda0, cfg.omega_k0, cfg.h0,
+                               workers=cores)
+        p, v = x.astype(np.float32), vv.astype(np.float32)
+        a += cfg.da
+    t = time.perf_counter() - t0
+    return {"value": cfg.np_total * steps / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} full-size step(s) (256^3 particles, 512^3 grid) of the FP64 numpy/scipy port, "
+                      f"FFTs on {cores} threads, particle loops vectorised single-threaded",
+            "seconds": round(t, 2)}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import numpy as np  # noqa: F401
+    K = max(1, min(args.steps, args.cpu_steps))
+    cfg = workload_config(K, args.n_parts, args.n_cells, args.box)
+    pos, vel = make_ics(cfg)
+    if args.warmup > 0:
+        cpu_baseline(cfg, pos, vel, 1)
+    cb = cpu_baseline(cfg, pos, vel, K)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws, "steps": K,
+            "warmup": min(args.warmup, 1), "ms_per_step": cb["seconds"] * 1e3 / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded GRF + Zel'dovich ICs (reference algorithm)",
+            "config": {"workload": WORKLOAD, "n_parts": 256, "n_cells": 512, "box_size": 250.0,
+                       "note": "numba/pyFFTW are not installed: the reference path runs as its FP64 "
+                               "numpy/scipy port; steps bounded to a few full-size steps"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=999)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--profile-steps", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-parts", type=int, default=256, help="reduced cases for profiling only")
+    ap.add_argument("--n-cells", type=int, default=512)
+    ap.add_argument("--box", type=float, default=250.0)
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

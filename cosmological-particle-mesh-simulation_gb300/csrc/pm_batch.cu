@@ -272,9 +272,16 @@ Work work_of(pm_batch* b, int ph, int total) {
   return w;
 }
 
-// Enqueue one step (state in b->st[cur] -> b->st[1 - cur]).
-int enqueue_step(pm_batch* b, int cur, cudaStream_t st) {
+// Phases timed by pm_batch_profile, in launch order.
+enum ProfPhase { PP_SORT = 0, PP_ROWS, PP_DEPOSIT, PP_X_R2C, PP_Y_FWD, PP_Z_GREEN, PP_Y_INV, PP_X_C2R, PP_KICK,
+                 PP_COEF, PP_COUNT };
+
+// Enqueue one step (state in b->st[cur] -> b->st[1 - cur]).  With `ev` (PP_COUNT + 1
+// events) an event is recorded before the first phase and after every phase.
+int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullptr) {
   Plan& P = b->plan;
+  auto mark = [&](int i) -> cudaError_t { return ev ? cudaEventRecord(ev[i], st) : cudaSuccess; };
+  PB_CK(mark(0), "event");
   const Sim* ds = b->d_sims.as<Sim>();
   int* err = b->d_err.as<int>();
   Parts in = state(b, cur), out = state(b, 1 - cur);
@@ -284,24 +291,38 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st) {
         "sort");
   unsigned* perm = alt ? b->sort.vals_alt.as<unsigned>() : b->sort.vals.as<unsigned>();
   unsigned* skeys = alt ? b->sort.keys_alt.as<unsigned>() : b->sort.keys.as<unsigned>();
+  PB_CK(mark(1 + PP_SORT), "event");
   PB_CK(launch_row_start(skeys, P.ptot, P.xbits, P.rows, b->row_start.as<unsigned>(), st), "rows");
+  PB_CK(mark(1 + PP_ROWS), "event");
   PB_CK(launch_deposit(ds, work_of(b, PH_DEP, P.fixed_total[PH_DEP]), in, perm, b->row_start.as<unsigned>(),
                        POS_DISP, err, grid_for(P.fixed_total[PH_DEP], b->sms, 8), P.max_dep_smem, st),
         "deposit");
+  PB_CK(mark(1 + PP_DEPOSIT), "event");
   const SpecKind order[5] = {SPEC_X_R2C, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Y_INV, SPEC_X_C2R};
-  for (SpecKind k : order) {
+  for (int o = 0; o < 5; ++o) {
+    const SpecKind k = order[o];
     for (size_t g = 0; g < P.sizes.size(); ++g) {
       const bool xk = (k == SPEC_X_R2C || k == SPEC_X_C2R);
       const int ph = PH_FIXED + 2 * (int)g + (xk ? 0 : 1);
       const int tot = xk ? P.x_total[g] : P.line_total[g];
       PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot), grid_for(tot, b->sms, 8), st), "spectral");
     }
+    PB_CK(mark(1 + PP_X_R2C + o), "event");
   }
   PB_CK(launch_kick(ds, work_of(b, PH_KICK, P.fixed_total[PH_KICK]), in, out, perm, b->sort.keys.as<unsigned>(),
                     POS_DISP, err, grid_for(P.fixed_total[PH_KICK], b->sms, 16), st),
         "kick");
+  PB_CK(mark(1 + PP_KICK), "event");
   PB_CK(launch_coef(b->d_sims.as<Sim>(), P.nsims, 1, st), "coef");
+  PB_CK(mark(1 + PP_COEF), "event");
   return PM_OK;
+}
+
+// Kernel launches of one step for the current plan.
+int launches_per_step(pm_batch* b) {
+  const Plan& P = b->plan;
+  const int passes = P.bits <= 0 ? 1 : (P.bits + 7) / 8;
+  return 3 * passes + 1 + 1 + 5 * (int)P.sizes.size() + 1 + 1;
 }
 
 int ensure_keys(pm_batch* b, cudaStream_t st) {
@@ -606,6 +627,48 @@ int pm_batch_remove(pm_batch* b, int sim_id) {
     }
   }
   return bfail(b, PM_ERR_ARG, "unknown simulation id");
+}
+
+int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void* stream) {
+  if (!b || !phase_ms || nphase < PP_COUNT) return PM_ERR_ARG;
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->own;
+  if (!stream) PB_CK(cudaDeviceSynchronize(), "sync");
+  for (int i = 0; i < nphase; ++i) phase_ms[i] = 0.f;
+  if (int r = retire_finished(b, st)) return r;
+  if (b->sims.empty()) return bfail(b, PM_ERR_ARG, "no active simulation");
+  if (b->dirty) {
+    if (int r = build_plan(b, st)) return r;
+  }
+  int k = nsteps;
+  for (auto& s : b->sims) k = std::min(k, s->nsteps - s->done);
+  if (int r = ensure_keys(b, st)) return r;
+  cudaEvent_t ev[PP_COUNT + 1];
+  for (auto& e : ev) PB_CK(cudaEventCreate(&e), "event");
+  int rc = PM_OK;
+  for (int i = 0; i < k && rc == PM_OK; ++i) {
+    rc = enqueue_step(b, b->cur, st, ev);
+    if (rc) break;
+    b->cur = 1 - b->cur;
+    for (auto& s : b->sims) { s->a += s->da; s->done += 1; }
+    cudaError_t e = cudaEventSynchronize(ev[PP_COUNT]);
+    if (e) { rc = bcuda(b, e, "profile sync"); break; }
+    for (int p = 0; p < PP_COUNT; ++p) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[p], ev[p + 1]);
+      phase_ms[p] += ms / (float)k;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (rc) return rc;
+  return retire_finished(b, st);
+}
+
+int pm_batch_launches_per_step(pm_batch* b) {
+  if (!b) return -1;
+  if (b->dirty && !b->sims.empty()) {
+    if (build_plan(b, b->own)) return -1;
+  }
+  return b->sims.empty() ? 0 : launches_per_step(b);
 }
 
 int pm_batch_check(pm_batch* b, void* stream, int* bits) {

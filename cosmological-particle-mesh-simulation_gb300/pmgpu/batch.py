@@ -104,6 +104,16 @@ class Batch:
         self._check(self._lib.pm_batch_remove(self._h, sid))
         self.cfgs.pop(sid, None)
 
+    def profile(self, nsteps: int) -> dict:
+        """Run up to nsteps steps with CUDA events between phases; mean ms per phase."""
+        arr = (ctypes.c_float * len(_lib.PROFILE_PHASES))()
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self._check(self._lib.pm_batch_profile(self._h, int(nsteps), arr, len(arr), stream))
+        return dict(zip(_lib.PROFILE_PHASES, [float(x) for x in arr]))
+
+    def launches_per_step(self) -> int:
+        return int(self._lib.pm_batch_launches_per_step(self._h))
+
     def check_device(self):
         bits = ctypes.c_int(0)
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)

@@ -136,6 +136,12 @@ int pm_batch_remove(pm_batch* b, int sim_id);
 int pm_batch_set_graphs(pm_batch* b, int enable);
 /* Device check bits of the batch (synchronises). */
 int pm_batch_check(pm_batch* b, void* stream, int* bits);
+/* Runs up to nsteps steps with direct launches and CUDA events between phases, and
+   writes the mean milliseconds of each phase to phase_ms[0..9]: sort, row starts,
+   deposit, x R2C, y forward, z Green, y inverse, x C2R, kick/drift, coefficients. */
+int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void* stream);
+/* Kernel launches per step for the resident simulations (-1 on error). */
+int pm_batch_launches_per_step(pm_batch* b);
 
 #ifdef __cplusplus
 }

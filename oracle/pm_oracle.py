@@ -190,12 +190,20 @@ def fourier_grid(n):
     return out
 
 
-def potential(density, fgrid, a, omega_m0):
+def potential(density, fgrid, a, omega_m0, workers=None):
     """potential.py:7-29: complex128 forward FFT, x(-3 Om/(8a) fgrid), normalised
-    backward FFT, real part."""
-    rho_k = np.fft.fftn(np.asarray(density, dtype=np.complex128))
+    backward FFT, real part.  ``workers`` threads the FFTs through scipy.fft (the
+    reference threads FFTW with N_CPU)."""
+    if workers:
+        import scipy.fft as sfft
+        fftn = lambda x: sfft.fftn(x, workers=workers)  # noqa: E731
+        ifftn = lambda x: sfft.ifftn(x, workers=workers)  # noqa: E731
+    else:
+        fftn, ifftn = np.fft.fftn, np.fft.ifftn
+    rho_k = fftn(np.asarray(density, dtype=np.complex128))
     phi_k = -3.0 * omega_m0 / 8.0 / a * np.asarray(fgrid, dtype=np.float64) * rho_k
-    return np.fft.ifftn(phi_k).real
+    del rho_k
+    return ifftn(phi_k).real
 
 
 # --------------------------------------------------------------------------------------
@@ -242,9 +250,9 @@ def integrate(positions, velocities, a_val, f_a1, da, phi, canonical=True):
 
 
 def advance_time(density, positions, velocities, fgrid, a, da, omega_m0, omega_lambda0,
-                 omega_k0, h0, fix_cosmo_f=False, canonical=True):
+                 omega_k0, h0, fix_cosmo_f=False, canonical=True, workers=None):
     """integrate.py:9-13."""
-    phi = potential(density, fgrid, a, omega_m0)
+    phi = potential(density, fgrid, a, omega_m0, workers=workers)
     cos = [omega_m0 if fix_cosmo_f else h0, omega_lambda0, omega_k0]
     fa1 = cosmo_f(a + da, cos)
     return integrate(positions, velocities, a, fa1, da, phi, canonical)
