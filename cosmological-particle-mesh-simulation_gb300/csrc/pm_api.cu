@@ -116,7 +116,7 @@ int sort_particles(pm_ctx* c, Call& k, cudaStream_t st, unsigned** perm, unsigne
   const long long nrows = (long long)c->n * c->n;
   const int bits = ceil_log2(nrows) + k.sim.xbits;
   bool alt = false;
-  PM_CK(radix_sort(c->sort.keys.as<unsigned>(), c->sort.vals.as<unsigned>(), np, bits, true,
+  PM_CK(radix_sort(c->sort.keys.as<unsigned>(), c->sort.vals.as<unsigned>(), np, 0, bits, true,
                    c->sort.scratch(), &alt, st),
         "sort");
   *perm = alt ? c->sort.vals_alt.as<unsigned>() : c->sort.vals.as<unsigned>();
@@ -140,11 +140,14 @@ int spectral(pm_ctx* c, Call& k, bool table, cudaStream_t st) {
   const Sim* ds = c->d_sim.as<Sim>();
   const int n = c->n;
   const int gx = grid_for(k.prefix[PH_X][1], c->sms, 8), gl = grid_for(k.prefix[PH_LINE][1], c->sms, 8);
-  PM_CK(spectral_dispatch(SPEC_X_R2C, n, ds, work(c, k, PH_X), gx, st), "x r2c");
-  PM_CK(spectral_dispatch(SPEC_Y_FWD, n, ds, work(c, k, PH_LINE), gl, st), "y fwd");
-  PM_CK(spectral_dispatch(table ? SPEC_Z_TABLE : SPEC_Z_GREEN, n, ds, work(c, k, PH_LINE), gl, st), "z green");
-  PM_CK(spectral_dispatch(SPEC_Y_INV, n, ds, work(c, k, PH_LINE), gl, st), "y inv");
-  PM_CK(spectral_dispatch(SPEC_X_C2R, n, ds, work(c, k, PH_X), gx, st), "x c2r");
+  const void* sp = k.sim.spec;
+  int* err = c->d_err.as<int>();
+  PM_CK(spectral_dispatch(SPEC_X_R2C, n, ds, work(c, k, PH_X), gx, st, sp, 0, err), "x r2c");
+  PM_CK(spectral_dispatch(SPEC_Y_FWD, n, ds, work(c, k, PH_LINE), gl, st, sp, 0, err), "y fwd");
+  PM_CK(spectral_dispatch(table ? SPEC_Z_TABLE : SPEC_Z_GREEN, n, ds, work(c, k, PH_LINE), gl, st, sp, 0, err),
+        "z green");
+  PM_CK(spectral_dispatch(SPEC_Y_INV, n, ds, work(c, k, PH_LINE), gl, st, sp, 0, err), "y inv");
+  PM_CK(spectral_dispatch(SPEC_X_C2R, n, ds, work(c, k, PH_X), gx, st, sp, 0, err), "x c2r");
   return PM_OK;
 }
 

@@ -44,6 +44,7 @@ struct Plan {
   std::vector<int> sizes;  // distinct grid sizes
   int fixed_total[PH_FIXED]{};
   std::vector<int> x_total, line_total;  // per distinct size
+  std::vector<int> single;               // per distinct size: the only simulation of that size, or -1
   int max_dep_smem = 0;
 };
 
@@ -248,6 +249,10 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   for (size_t g = 0; g < P.sizes.size(); ++g) {
     P.x_total.push_back(at(PH_FIXED + 2 * (int)g, S));
     P.line_total.push_back(at(PH_FIXED + 2 * (int)g + 1, S));
+    int only = -1, count = 0;
+    for (int i = 0; i < S; ++i)
+      if (b->sims[i]->n == P.sizes[g]) { only = i; ++count; }
+    P.single.push_back(count == 1 ? only : -1);
   }
   PB_CK(b->d_sims.ensure(sizeof(Sim) * S), "alloc sims");
   PB_CK(b->d_prefix.ensure(sizeof(int) * pre.size()), "alloc prefix");
@@ -286,8 +291,11 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
   int* err = b->d_err.as<int>();
   Parts in = state(b, cur), out = state(b, 1 - cur);
   bool alt = false;
-  PB_CK(radix_sort(b->sort.keys.as<unsigned>(), b->sort.vals.as<unsigned>(), P.ptot, P.bits, true,
-                   b->sort.scratch(), &alt, st),
+  // the deposit needs particles grouped by x-row only (its sums do not depend on the order
+  // inside a row): sort on the row bits of the key; the sort is stable, so the order inside
+  // a row is the previous step's order, itself sorted by cell
+  PB_CK(radix_sort(b->sort.keys.as<unsigned>(), b->sort.vals.as<unsigned>(), P.ptot, P.xbits, P.bits - P.xbits,
+                   true, b->sort.scratch(), &alt, st),
         "sort");
   unsigned* perm = alt ? b->sort.vals_alt.as<unsigned>() : b->sort.vals.as<unsigned>();
   unsigned* skeys = alt ? b->sort.keys_alt.as<unsigned>() : b->sort.keys.as<unsigned>();
@@ -305,7 +313,11 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
       const bool xk = (k == SPEC_X_R2C || k == SPEC_X_C2R);
       const int ph = PH_FIXED + 2 * (int)g + (xk ? 0 : 1);
       const int tot = xk ? P.x_total[g] : P.line_total[g];
-      PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot), grid_for(tot, b->sms, 8), st), "spectral");
+      const int one = P.single[g];
+      const void* sp = one >= 0 ? b->sims[one]->spec.p : nullptr;
+      PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot), grid_for(tot, b->sms, 8), st, sp,
+                              one >= 0 ? one : 0, err),
+            "spectral");
     }
     PB_CK(mark(1 + PP_X_R2C + o), "event");
   }
@@ -321,7 +333,7 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
 // Kernel launches of one step for the current plan.
 int launches_per_step(pm_batch* b) {
   const Plan& P = b->plan;
-  const int passes = P.bits <= 0 ? 1 : (P.bits + 7) / 8;
+  const int passes = radix_sort_passes(P.bits - P.xbits);
   return 3 * passes + 1 + 1 + 5 * (int)P.sizes.size() + 1 + 1;
 }
 

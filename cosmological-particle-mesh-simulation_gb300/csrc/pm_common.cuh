@@ -22,6 +22,7 @@ enum : int {
   ERR_CELL_RANGE = 1,   // a particle cell fell outside the grid (NaN/Inf position)
   ERR_SOURCE_ROW = 2,   // deposit: particle outside the tile's source rows (sort broken)
   ERR_NONFINITE = 4,    // kick/drift produced a non-finite coordinate
+  ERR_TIMEOUT = 8,      // a bounded wait on an asynchronous copy gave up
 };
 
 enum PosMode : int { POS_ABS = 0, POS_DISP = 1 };
@@ -90,14 +91,20 @@ __device__ __forceinline__ void set_error(int* err, int code) {
 // spectral passes: one kernel per grid size n (supported n: spectral_supported)
 enum SpecKind : int { SPEC_X_R2C = 0, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Z_TABLE, SPEC_Y_INV, SPEC_X_C2R,
                       SPEC_PREPARE /* only set kernel attributes */ };
+// spec_single: the spectrum of the only simulation of size N in the launch, sims[sim_index]
+// (enables the TMA-streamed line passes for the sizes that have them); nullptr when
+// several simulations of size N share the launch.  The other kernels ignore both and
+// find their simulation through the work prefix.
 template <int N>
-cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cudaStream_t st);
+cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cudaStream_t st,
+                            const void* spec_single, int sim_index, int* err);
 bool spectral_supported(int n);
 // work units (CTAs' worth of work) of one spectral pass for a grid of size n
 long long spectral_units(SpecKind kind, int n);
 // resident CTAs per SM of a spectral pass for size n (for persistent grid sizing)
 int spectral_ctas_per_sm(SpecKind kind, int n);
-cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int ctas, cudaStream_t st);
+cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int ctas, cudaStream_t st,
+                              const void* spec_single = nullptr, int sim_index = 0, int* err = nullptr);
 cudaError_t launch_fourier_grid(const Sim* sims, int ctas, cudaStream_t st);
 
 // particle kernels
@@ -121,7 +128,7 @@ cudaError_t launch_disp_to_abs(Parts in, long long off, long long np, int np1, i
                                const float* q_frac, float* pos, float* vel, cudaStream_t st);
 size_t deposit_smem_bytes(int n, int ty, int tz);
 
-// radix sort of (key, value) pairs, stable, LSD, 8-bit digits
+// radix sort of (key, value) pairs, stable, LSD, digits of up to 9 bits
 struct SortScratch {
   unsigned* keys_alt; unsigned* vals_alt;
   unsigned* hist;     // 256 * max_blocks
@@ -130,10 +137,12 @@ struct SortScratch {
 };
 constexpr int SORT_TILE = 4096;
 size_t sort_scratch_hist_entries(long long n);
-// Sorts keys[0,n) / vals[0,n) on bits [0, bits).  Returns via *in_alt whether the result
-// sits in the scratch (alt) buffers.  When gen_vals is set, vals are not read on the
-// first pass and the identity 0..n-1 is used instead.
-cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int bits, bool gen_vals,
+constexpr int SORT_DIGIT_TOTALS = 512;  // entries of SortScratch::digit_tot
+int radix_sort_passes(int bits);
+// Sorts keys[0,n) / vals[0,n) on key bits [begin_bit, begin_bit + bits).  Returns via
+// *in_alt whether the result sits in the scratch (alt) buffers.  When gen_vals is set,
+// vals are not read on the first pass and the identity 0..n-1 is used instead.
+cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int begin_bit, int bits, bool gen_vals,
                        const SortScratch& s, bool* in_alt, cudaStream_t st);
 
 }  // namespace pm

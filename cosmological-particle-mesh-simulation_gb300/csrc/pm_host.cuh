@@ -109,7 +109,7 @@ struct SortBufs {
     if (!e) e = keys_alt.ensure(b);
     if (!e) e = vals_alt.ensure(b);
     if (!e) e = hist.ensure(sort_scratch_hist_entries(n) * sizeof(unsigned));
-    if (!e) e = digit_tot.ensure(256 * sizeof(unsigned));
+    if (!e) e = digit_tot.ensure(SORT_DIGIT_TOTALS * sizeof(unsigned));
     if (!e) cap = n;
     return e;
   }
@@ -120,7 +120,7 @@ struct SortBufs {
     s.hist = hist.as<unsigned>();
     s.digit_tot = digit_tot.as<unsigned>();
     s.capacity = cap;
-    s.max_blocks = (int)(hist.bytes / sizeof(unsigned) / 256);
+    s.max_blocks = (int)(hist.bytes / sizeof(unsigned) / SORT_DIGIT_TOTALS);
     return s;
   }
   void release() {

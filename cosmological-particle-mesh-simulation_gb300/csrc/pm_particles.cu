@@ -9,8 +9,11 @@
 //            potential.py:15, cosmology.py:20-27)
 //
 // Cell key = (global x-row number << xbits) | x, where x-rows are numbered in
-// deposit-tile order (a tile is tz planes x ty rows of full x-rows).  Sorting by key
-// groups particles by tile and, inside a tile, by cell.
+// deposit-tile order (a tile is TZ planes x TY rows of full x-rows, TY = TZ = 4).
+// Sorting by key groups particles by tile and, inside a tile, by cell.
+//
+// Resident (displacement) particles carry their Lagrangian lattice index packed as
+// ix << 20 | iy << 10 | iz (N_PARTS <= 1024), so no division is needed to find q.
 #include "pm_common.cuh"
 
 namespace pm {
@@ -19,13 +22,18 @@ constexpr int DEP_NT = 256;
 constexpr int KICK_NT = 256;
 constexpr int KEY_NT = 256;
 constexpr unsigned FULL = 0xffffffffu;
+constexpr int TY = 4, TZ = 4, NSRC = (TY + 1) * (TZ + 1);
+
+__host__ __device__ __forceinline__ unsigned pack_lattice(unsigned ix, unsigned iy, unsigned iz) {
+  return (ix << 20) | (iy << 10) | iz;
+}
 
 // ---------------------------------------------------------------------------------
 // cells
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ unsigned row_number(int y, int z, int n, int ty, int tz) {
-  const unsigned tile = (unsigned)(z / tz) * (unsigned)(n / ty) + (unsigned)(y / ty);
-  return tile * (unsigned)(tz * ty) + (unsigned)((z % tz) * ty + (y % ty));
+__device__ __forceinline__ unsigned row_number(int y, int z, int n) {
+  const unsigned tile = (unsigned)(z / TZ) * (unsigned)(n / TY) + (unsigned)(y / TY);
+  return tile * (unsigned)(TZ * TY) + (unsigned)((z % TZ) * TY + (y % TY));
 }
 
 // Q4: a float32 coordinate equal to n (or slightly negative) is mapped into [0, n).
@@ -56,6 +64,9 @@ __device__ __forceinline__ Cell cell_abs(float x, float y, float z, int n) {
 }
 
 __device__ __forceinline__ int wrap_int(int c, int n) {
+  if ((unsigned)c < (unsigned)n) return c;
+  if (c >= n && c < 2 * n) return c - n;
+  if (c < 0 && c >= -n) return c + n;
   c %= n;
   return c < 0 ? c + n : c;
 }
@@ -63,8 +74,7 @@ __device__ __forceinline__ int wrap_int(int c, int n) {
 // displacement from the Lagrangian lattice point -> cell:
 //   cell = (q_int + floor(q_frac + d)) mod n,  offset = (q_frac + d) - floor(q_frac + d)
 __device__ __forceinline__ Cell cell_disp(const Sim& S, unsigned id, float dx, float dy, float dz) {
-  const unsigned np1 = (unsigned)S.np1;
-  const unsigned ix = id / (np1 * np1), iy = (id / np1) % np1, iz = id % np1;
+  const unsigned ix = id >> 20, iy = (id >> 10) & 1023u, iz = id & 1023u;
   const float sx = __ldg(&S.q_frac[ix]) + dx;
   const float sy = __ldg(&S.q_frac[iy]) + dy;
   const float sz = __ldg(&S.q_frac[iz]) + dz;
@@ -87,7 +97,7 @@ __device__ __forceinline__ Cell particle_cell(const Sim& S, const Parts& p, long
 }
 
 __device__ __forceinline__ unsigned cell_key(const Sim& S, const Cell& c) {
-  return ((S.row_base + row_number(c.y, c.z, S.n, S.ty, S.tz)) << S.xbits) | (unsigned)c.x;
+  return ((S.row_base + row_number(c.y, c.z, S.n)) << S.xbits) | (unsigned)c.x;
 }
 
 // The 8 CIC weights in the order of integrate.py:44-51: [ttt, dtt, tdt, ttd, ddt, dtd, tdd, ddd]
@@ -146,98 +156,111 @@ __global__ void k_row_start(const unsigned* __restrict__ keys, long long n, int 
 //
 // One CTA per deposit tile (tz x ty full x-rows).  It gathers every particle whose base
 // cell lies in the tile's source rows (the tile plus one row/plane below, periodic),
-// adds the CIC weights that land inside the tile to 64-bit integer accumulators in
-// shared memory (weights quantised to 2^-26: integer adds commute, so the result is
-// the same whatever the order of the atomics), then writes the tile's rows once.
-// Lanes of a warp that share a cell are combined with one warp reduction first.
+// adds the CIC weights that land inside the tile to integer accumulators in shared
+// memory (weights quantised to 2^-26; a 32-bit low word with carry into a 32-bit high
+// word, so the sum is exact and independent of the order of the atomics), then writes
+// the tile's rows once.  Lanes that hit the same cell in one atomic instruction are
+// serialised by the hardware; their integer sum is the same in any order.
 // ---------------------------------------------------------------------------------
+__device__ __forceinline__ void acc_add(unsigned* lo, unsigned* hi, int i, unsigned q) {
+  const unsigned old = atomicAdd(&lo[i], q);
+  if (old + q < old) atomicAdd(&hi[i], 1u);
+}
+
+__device__ __forceinline__ float fixed_to_float(unsigned l, unsigned h, float scale) {
+  return (h == 0u ? __uint2float_rn(l) : __ull2float_rn(((unsigned long long)h << 32) | l)) * scale;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(DEP_NT) k_deposit(const Sim* __restrict__ sims, Work w, Parts p,
                                                     const unsigned* __restrict__ perm,
                                                     const unsigned* __restrict__ row_start, int* err) {
-  extern __shared__ unsigned long long acc[];
-  __shared__ unsigned s_begin[32];
-  __shared__ unsigned s_off[33];
+  extern __shared__ uint4 acc_raw[];
+  __shared__ unsigned s_begin[NSRC];
+  __shared__ unsigned s_off[NSRC + 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
     const int si = locate_sim(w, unit);
     const Sim& S = sims[si];
     const int local = unit - __ldg(&w.prefix[si]);
-    const int n = S.n, ty = S.ty, tz = S.tz;
-    const int ntile_y = n / ty;
-    const int y0 = (local % ntile_y) * ty, z0 = (local / ntile_y) * tz;
-    const int ncell = tz * ty * n;
-    const int nsrc = (tz + 1) * (ty + 1);
-    for (int i = threadIdx.x; i < ncell; i += DEP_NT) acc[i] = 0ull;
-    if (threadIdx.x < nsrc) {
-      const int lz = threadIdx.x / (ty + 1) - 1, ly = threadIdx.x % (ty + 1) - 1;
-      const int z = (z0 + lz + n) % n, y = (y0 + ly + n) % n;
-      const unsigned r = S.row_base + row_number(y, z, n, ty, tz);
-      const unsigned b = __ldg(&row_start[r]);
-      s_begin[threadIdx.x] = b;
-      s_off[threadIdx.x + 1] = __ldg(&row_start[r + 1]) - b;
+    const int n = S.n;
+    const int ntile_y = n / TY;
+    const int y0 = (local % ntile_y) * TY, z0 = (local / ntile_y) * TZ;
+    const int ncell = TZ * TY * n;  // a multiple of 64
+    unsigned* lo = reinterpret_cast<unsigned*>(acc_raw);
+    unsigned* hi = lo + ncell;
+    for (int i = threadIdx.x; i < ncell / 2; i += DEP_NT) acc_raw[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (warp == 0) {
+      // source rows (lz, ly) in [-1, TZ-1] x [-1, TY-1]: begin and an inclusive scan of counts
+      unsigned beg = 0, cnt = 0;
+      if (lane < NSRC) {
+        const int lz = lane / (TY + 1) - 1, ly = lane % (TY + 1) - 1;
+        const int z = z0 + lz < 0 ? z0 + lz + n : z0 + lz;
+        const int y = y0 + ly < 0 ? y0 + ly + n : y0 + ly;
+        const unsigned r = S.row_base + row_number(y, z, n);
+        beg = __ldg(&row_start[r]);
+        cnt = __ldg(&row_start[r + 1]) - beg;
+      }
+      unsigned incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+      }
+      if (lane < NSRC) {
+        s_begin[lane] = beg;
+        s_off[lane + 1] = incl;
+      }
+      if (lane == 0) s_off[0] = 0;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      s_off[0] = 0;
-      for (int r = 1; r <= nsrc; ++r) s_off[r] += s_off[r - 1];
-    }
-    __syncthreads();
-    const unsigned total = s_off[nsrc];
+    const unsigned total = s_off[NSRC];
     for (unsigned base = (unsigned)warp * 32u; base < total; base += DEP_NT) {
       const unsigned f = base + lane;
       const bool valid = f < total;
       float wt[8];
       int cx = 0, ly = 0, lz = 0;
-      unsigned ckey = 0x80000000u | (unsigned)lane;  // unique key of an idle lane
       bool ok = false;
       if (valid) {
-        int r = 0;
-        while (r + 1 < nsrc && s_off[r + 1] <= f) ++r;
+        int r = 0;  // last source row with s_off[r] <= f
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+          if (r + step < NSRC && s_off[r + step] <= f) r += step;
         const unsigned slot = __ldg(&perm[s_begin[r] + (f - s_off[r])]);
         const Cell c = particle_cell<MODE>(S, p, slot);
         int dy = c.y - y0, dz = c.z - z0;
         if (dy >= n - 1) dy -= n;
         if (dz >= n - 1) dz -= n;
-        ok = c.ok && dy >= -1 && dy < ty && dz >= -1 && dz < tz;
+        ok = c.ok && dy >= -1 && dy < TY && dz >= -1 && dz < TZ;
         if (!ok) {
           set_error(err, c.ok ? ERR_SOURCE_ROW : ERR_CELL_RANGE);
         } else {
           cic_weights(c, wt);
           cx = c.x; ly = dy; lz = dz;
-          ckey = (unsigned)(((lz + 1) * (ty + 1) + (ly + 1)) * n + cx);
         }
       }
-      unsigned q[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) q[k] = ok ? __float2uint_rn(wt[k] * (float)(1u << PM_FIX_BITS)) : 0u;
-      const unsigned prev = __shfl_up_sync(FULL, ckey, 1);
-      const bool dup = __any_sync(FULL, lane > 0 && prev == ckey);
-      bool lead = ok;
-      if (dup) {
-        const unsigned peers = __match_any_sync(FULL, ckey);
-#pragma unroll
-        for (int k = 0; k < 8; ++k) q[k] = __reduce_add_sync(peers, q[k]);
-        lead = ok && lane == __ffs(peers) - 1;
-      }
-      if (lead) {
+      if (ok) {
+        const int x1 = cx + 1 == n ? 0 : cx + 1;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
           const int ty2 = ly + c_corner[k][1], tz2 = lz + c_corner[k][2];
-          if (ty2 >= 0 && ty2 < ty && tz2 >= 0 && tz2 < tz) {
-            int x2 = cx + c_corner[k][0];
-            if (x2 == n) x2 = 0;
-            atomicAdd(&acc[(tz2 * ty + ty2) * n + x2], (unsigned long long)q[k]);
-          }
+          if (ty2 >= 0 && ty2 < TY && tz2 >= 0 && tz2 < TZ)
+            acc_add(lo, hi, (tz2 * TY + ty2) * n + (c_corner[k][0] ? x1 : cx),
+                    __float2uint_rn(wt[k] * (float)(1u << PM_FIX_BITS)));
         }
       }
     }
     __syncthreads();
     const float ms = S.mass_scale;
-    for (int i = threadIdx.x; i < ncell; i += DEP_NT) {
-      const int x = i % n, row = i / n;
-      const int ly2 = row % ty, lz2 = row / ty;
-      S.rho[((long long)(z0 + lz2) * n + (y0 + ly2)) * n + x] = __ull2float_rn(acc[i]) * ms;
+    for (int row = warp; row < TZ * TY; row += DEP_NT / 32) {
+      const uint4* l4 = reinterpret_cast<const uint4*>(lo + row * n);
+      const uint4* h4 = reinterpret_cast<const uint4*>(hi + row * n);
+      float4* dst = reinterpret_cast<float4*>(S.rho + ((long long)(z0 + row / TY) * n + (y0 + row % TY)) * n);
+      for (int x4 = lane; x4 < n / 4; x4 += 32) {
+        const uint4 l = l4[x4], h = h4[x4];
+        dst[x4] = make_float4(fixed_to_float(l.x, h.x, ms), fixed_to_float(l.y, h.y, ms),
+                              fixed_to_float(l.z, h.z, ms), fixed_to_float(l.w, h.w, ms));
+      }
     }
     __syncthreads();
   }
@@ -400,7 +423,7 @@ __global__ void k_abs_to_disp(const float* __restrict__ pos, const float* __rest
       dst[k][off + i] = d;
       vdst[k][off + i] = vel[k * np + i];
     }
-    out.id[off + i] = id;
+    out.id[off + i] = pack_lattice(ax[0], ax[1], ax[2]);
   }
 }
 
@@ -411,8 +434,9 @@ __global__ void k_disp_to_abs(Parts in, long long off, long long np, int np1, in
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < np;
        j += (long long)gridDim.x * blockDim.x) {
     const long long slot = off + j;
-    const unsigned id = in.id[slot], u1 = (unsigned)np1;
-    const unsigned ax[3] = {id / (u1 * u1), (id / u1) % u1, id % u1};
+    const unsigned pid = in.id[slot];
+    const unsigned ax[3] = {pid >> 20, (pid >> 10) & 1023u, pid & 1023u};
+    const long long id = ((long long)ax[0] * np1 + ax[1]) * np1 + ax[2];
     const float dv[3] = {in.x[slot], in.y[slot], in.z[slot]};
     const float vv[3] = {in.vx[slot], in.vy[slot], in.vz[slot]};
 #pragma unroll
@@ -452,6 +476,8 @@ cudaError_t deposit_prepare() {
                                        (int)deposit_smem_bytes(PM_MAX_N, 4, 4));
   if (!e) e = cudaFuncSetAttribute(k_deposit<POS_DISP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)deposit_smem_bytes(PM_MAX_N, 4, 4));
+  if (!e) e = cudaFuncSetAttribute(k_deposit<POS_ABS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (!e) e = cudaFuncSetAttribute(k_deposit<POS_DISP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   return e;
 }
 

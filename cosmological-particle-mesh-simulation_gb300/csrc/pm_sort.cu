@@ -1,4 +1,4 @@
-// Stable LSD radix sort of (key, value) pairs, 8-bit digits, reduce-then-scan.
+// Stable LSD radix sort of (key, value) pairs, digits of up to 9 bits, reduce-then-scan.
 //
 // Per digit pass:
 //   upsweep    per-tile digit histogram            hist[d * nblocks + tile]
@@ -7,7 +7,8 @@
 //              multisplit, warps in tile order, batches in order), staging in shared
 //              memory by digit, coalesced write to digit_base[d] + tile_offset + rank
 //
-// Only integer arithmetic: the output is bit-exact and independent of scheduling.
+// A sort over `bits` key bits takes ceil(bits / 9) passes of equal width.  Only integer
+// arithmetic: the output is bit-exact and independent of scheduling.
 #include "pm_common.cuh"
 
 namespace pm {
@@ -16,21 +17,32 @@ constexpr int SORT_NT = 256;
 constexpr int SORT_IPT = SORT_TILE / SORT_NT;  // 16 items per thread
 constexpr int SORT_WARPS = SORT_NT / 32;
 constexpr int SORT_SCAN_NT = 1024;
+constexpr int MAX_DIGIT_BITS = 9;
+constexpr int MAX_RADIX = 1 << MAX_DIGIT_BITS;
+constexpr int DPT = MAX_RADIX / SORT_NT;  // digits per thread in per-digit loops
 
 __global__ void __launch_bounds__(SORT_NT) k_sort_upsweep(const unsigned* __restrict__ keys, long long n,
-                                                          int shift, unsigned* __restrict__ hist, int nblocks) {
-  __shared__ unsigned h[SORT_WARPS][256];
+                                                          int shift, int dbits, unsigned* __restrict__ hist,
+                                                          int nblocks) {
+  __shared__ unsigned h[SORT_WARPS][MAX_RADIX];
   const int warp = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < SORT_WARPS * 256; i += SORT_NT) (&h[0][0])[i] = 0;
+  const unsigned mask = (1u << dbits) - 1u, radix = 1u << dbits;
+  for (int i = threadIdx.x; i < SORT_WARPS * MAX_RADIX; i += SORT_NT) (&h[0][0])[i] = 0;
   __syncthreads();
   const long long base = (long long)blockIdx.x * SORT_TILE;
-#pragma unroll 4
+  unsigned k[SORT_IPT];
+#pragma unroll
   for (int i = 0; i < SORT_IPT; ++i) {
     const long long idx = base + i * SORT_NT + threadIdx.x;
-    if (idx < n) atomicAdd(&h[warp][(__ldg(&keys[idx]) >> shift) & 255u], 1u);
+    k[i] = idx < n ? __ldg(&keys[idx]) : 0u;
+  }
+#pragma unroll
+  for (int i = 0; i < SORT_IPT; ++i) {
+    const long long idx = base + i * SORT_NT + threadIdx.x;
+    if (idx < n) atomicAdd(&h[warp][(k[i] >> shift) & mask], 1u);
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += SORT_NT) {
+  for (unsigned d = threadIdx.x; d < radix; d += SORT_NT) {
     unsigned s = 0;
 #pragma unroll
     for (int w = 0; w < SORT_WARPS; ++w) s += h[w][d];
@@ -38,7 +50,7 @@ __global__ void __launch_bounds__(SORT_NT) k_sort_upsweep(const unsigned* __rest
   }
 }
 
-// Block-wide exclusive scan of one value per thread; returns the block total.
+// Block-wide exclusive scan of one value per thread; returns the block total in `total`.
 template <int NT>
 __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned* ws, unsigned& total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -82,28 +94,46 @@ __global__ void __launch_bounds__(SORT_SCAN_NT) k_sort_scan(unsigned* __restrict
   if (threadIdx.x == 0) digit_tot[blockIdx.x] = carry;
 }
 
+struct DownSmem {
+  unsigned skey[SORT_TILE];
+  unsigned sval[SORT_TILE];
+  unsigned wcnt[SORT_WARPS][MAX_RADIX];
+  unsigned dstart[MAX_RADIX];
+  unsigned gofs[MAX_RADIX];
+  unsigned ws[32];
+};
+
 __global__ void __launch_bounds__(SORT_NT) k_sort_downsweep(const unsigned* __restrict__ keys_in,
                                                             const unsigned* __restrict__ vals_in,
                                                             unsigned* __restrict__ keys_out,
                                                             unsigned* __restrict__ vals_out, long long n,
-                                                            int shift, const unsigned* __restrict__ hist,
+                                                            int shift, int dbits,
+                                                            const unsigned* __restrict__ hist,
                                                             const unsigned* __restrict__ digit_tot,
                                                             int nblocks, int gen_vals) {
-  __shared__ unsigned skey[SORT_TILE];
-  __shared__ unsigned sval[SORT_TILE];
-  __shared__ unsigned wcnt[SORT_WARPS][256];
-  __shared__ unsigned dstart[256];
-  __shared__ unsigned gofs[256];
-  __shared__ unsigned ws[32];
+  extern __shared__ uint4 down_raw[];
+  DownSmem& sm = *reinterpret_cast<DownSmem*>(down_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned mask = (1u << dbits) - 1u, radix = 1u << dbits;
   const long long base = (long long)blockIdx.x * SORT_TILE;
-  for (int i = threadIdx.x; i < SORT_WARPS * 256; i += SORT_NT) (&wcnt[0][0])[i] = 0;
-  // global start of each digit for this tile
+  for (int i = threadIdx.x; i < SORT_WARPS * MAX_RADIX; i += SORT_NT) (&sm.wcnt[0][0])[i] = 0;
+  // global start of each digit for this tile: exclusive scan of the digit totals
   {
-    const unsigned t = threadIdx.x < 256 ? digit_tot[threadIdx.x] : 0u;
+    unsigned t[DPT], s = 0;
+#pragma unroll
+    for (int j = 0; j < DPT; ++j) {
+      const unsigned d = threadIdx.x * DPT + j;
+      t[j] = d < radix ? digit_tot[d] : 0u;
+      s += t[j];
+    }
     unsigned tot;
-    const unsigned ex = block_exclusive_scan<SORT_NT>(t, ws, tot);
-    if (threadIdx.x < 256) gofs[threadIdx.x] = ex + hist[(long long)threadIdx.x * nblocks + blockIdx.x];
+    unsigned ex = block_exclusive_scan<SORT_NT>(s, sm.ws, tot);
+#pragma unroll
+    for (int j = 0; j < DPT; ++j) {
+      const unsigned d = threadIdx.x * DPT + j;
+      if (d < radix) sm.gofs[d] = ex + hist[(long long)d * nblocks + blockIdx.x];
+      ex += t[j];
+    }
   }
   __syncthreads();
   unsigned key[SORT_IPT], val[SORT_IPT], rank[SORT_IPT];
@@ -120,73 +150,96 @@ __global__ void __launch_bounds__(SORT_NT) k_sort_downsweep(const unsigned* __re
   for (int i = 0; i < SORT_IPT; ++i) {
     const long long idx = wbase + i * 32 + lane;
     const bool valid = idx < n;
-    const unsigned d = valid ? ((key[i] >> shift) & 255u) : 256u + lane;
+    const unsigned d = valid ? ((key[i] >> shift) & mask) : (unsigned)MAX_RADIX + lane;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
-    const unsigned prior = valid ? wcnt[warp][d] : 0u;
+    const unsigned prior = valid ? sm.wcnt[warp][d] : 0u;
     __syncwarp();
-    if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = prior + __popc(peers);
+    if (valid && lane == __ffs(peers) - 1) sm.wcnt[warp][d] = prior + __popc(peers);
     __syncwarp();
     rank[i] = prior + __popc(peers & lt_mask);
   }
   __syncthreads();
   // per digit: warp prefix counts and the tile-local digit start
   {
-    unsigned run = 0;
-    if (threadIdx.x < 256) {
+    unsigned run[DPT], s = 0;
 #pragma unroll
-      for (int w = 0; w < SORT_WARPS; ++w) {
-        const unsigned c = wcnt[w][threadIdx.x];
-        wcnt[w][threadIdx.x] = run;
-        run += c;
+    for (int j = 0; j < DPT; ++j) {
+      const unsigned d = threadIdx.x * DPT + j;
+      unsigned r = 0;
+      if (d < radix) {
+#pragma unroll
+        for (int w = 0; w < SORT_WARPS; ++w) {
+          const unsigned c = sm.wcnt[w][d];
+          sm.wcnt[w][d] = r;
+          r += c;
+        }
       }
+      run[j] = r;
+      s += r;
     }
     unsigned tot;
-    const unsigned ex = block_exclusive_scan<SORT_NT>(threadIdx.x < 256 ? run : 0u, ws, tot);
-    if (threadIdx.x < 256) dstart[threadIdx.x] = ex;
+    unsigned ex = block_exclusive_scan<SORT_NT>(s, sm.ws, tot);
+#pragma unroll
+    for (int j = 0; j < DPT; ++j) {
+      const unsigned d = threadIdx.x * DPT + j;
+      if (d < radix) sm.dstart[d] = ex;
+      ex += run[j];
+    }
   }
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < SORT_IPT; ++i) {
     const long long idx = wbase + i * 32 + lane;
     if (idx < n) {
-      const unsigned d = (key[i] >> shift) & 255u;
-      const unsigned p = dstart[d] + wcnt[warp][d] + rank[i];
-      skey[p] = key[i];
-      sval[p] = val[i];
+      const unsigned d = (key[i] >> shift) & mask;
+      const unsigned p = sm.dstart[d] + sm.wcnt[warp][d] + rank[i];
+      sm.skey[p] = key[i];
+      sm.sval[p] = val[i];
     }
   }
   __syncthreads();
   const long long rem = n - base;
   const int cnt = rem < SORT_TILE ? (int)rem : SORT_TILE;
   for (int p = threadIdx.x; p < cnt; p += SORT_NT) {
-    const unsigned k = skey[p];
-    const unsigned d = (k >> shift) & 255u;
-    const unsigned g = gofs[d] + (unsigned)p - dstart[d];
+    const unsigned k = sm.skey[p];
+    const unsigned d = (k >> shift) & mask;
+    const unsigned g = sm.gofs[d] + (unsigned)p - sm.dstart[d];
     keys_out[g] = k;
-    vals_out[g] = sval[p];
+    vals_out[g] = sm.sval[p];
   }
 }
 
 size_t sort_scratch_hist_entries(long long n) {
   const long long nb = (n + SORT_TILE - 1) / SORT_TILE;
-  return (size_t)256 * (nb > 0 ? nb : 1);
+  return (size_t)MAX_RADIX * (nb > 0 ? nb : 1);
 }
 
-cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int bits, bool gen_vals,
+int radix_sort_passes(int bits) { return bits <= 0 ? 1 : (bits + MAX_DIGIT_BITS - 1) / MAX_DIGIT_BITS; }
+
+cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int begin_bit, int bits, bool gen_vals,
                        const SortScratch& s, bool* in_alt, cudaStream_t st) {
   *in_alt = false;
   if (n <= 0) return cudaSuccess;
   if (n > s.capacity || n >= (1ll << 32)) return cudaErrorInvalidValue;
   const int nblocks = (int)((n + SORT_TILE - 1) / SORT_TILE);
   if (nblocks > s.max_blocks) return cudaErrorInvalidValue;
-  const int passes = bits <= 0 ? 1 : (bits + 7) / 8;
+  static bool init = false;
+  if (!init) {
+    cudaError_t e = cudaFuncSetAttribute(k_sort_downsweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(DownSmem));
+    if (e) return e;
+    init = true;
+  }
+  const int passes = radix_sort_passes(bits);
+  const int dbits = bits <= 0 ? 1 : (bits + passes - 1) / passes;
   unsigned *ki = keys, *vi = vals, *ko = s.keys_alt, *vo = s.vals_alt;
   for (int p = 0; p < passes; ++p) {
-    const int shift = 8 * p;
-    k_sort_upsweep<<<nblocks, SORT_NT, 0, st>>>(ki, n, shift, s.hist, nblocks);
-    k_sort_scan<<<256, SORT_SCAN_NT, 0, st>>>(s.hist, nblocks, s.digit_tot);
-    k_sort_downsweep<<<nblocks, SORT_NT, 0, st>>>(ki, vi, ko, vo, n, shift, s.hist, s.digit_tot, nblocks,
-                                                  (p == 0 && gen_vals) ? 1 : 0);
+    const int shift = begin_bit + dbits * p;
+    k_sort_upsweep<<<nblocks, SORT_NT, 0, st>>>(ki, n, shift, dbits, s.hist, nblocks);
+    k_sort_scan<<<1 << dbits, SORT_SCAN_NT, 0, st>>>(s.hist, nblocks, s.digit_tot);
+    k_sort_downsweep<<<nblocks, SORT_NT, sizeof(DownSmem), st>>>(ki, vi, ko, vo, n, shift, dbits, s.hist,
+                                                                 s.digit_tot, nblocks,
+                                                                 (p == 0 && gen_vals) ? 1 : 0);
     cudaError_t e = cudaGetLastError();
     if (e) return e;
     unsigned* t = ki; ki = ko; ko = t;

@@ -11,8 +11,11 @@
 // compiled with -DPM_N=<N>), so that register allocation is per size and the build
 // runs in parallel.
 #pragma once
+#include <cudaTypedefs.h>
+
 #include "pm_common.cuh"
 #include "pm_fft.cuh"
+#include "pm_tma.cuh"
 
 namespace pm {
 
@@ -35,11 +38,30 @@ __host__ __device__ constexpr int cbundles_per_plane(int n) {
   return (chalf(n) + cline_width(n) - 1) / cline_width(n);
 }
 
+__host__ __device__ constexpr int cpitch(int n) { return (chalf(n) + 15) / 16 * 16; }
+// Line passes that stream through a TMA ring: one bundle per unit, whole 256-row boxes.
+__host__ __device__ constexpr bool tma_lines(int n) { return cline_bpc(n) == 1 && n % 256 == 0; }
+constexpr int TMA_NT = 512;
+constexpr int TMA_STAGES = 3;
+__host__ __device__ constexpr size_t tma_stage_bytes(int n) { return (size_t)n * cline_width(n) * sizeof(float2); }
+__host__ __device__ constexpr size_t tma_smem_bytes(int n) { return TMA_STAGES * tma_stage_bytes(n) + 64; }
+
+// x passes fed by bulk copies into a double-buffered staging area (one simulation per launch)
+__host__ __device__ constexpr bool tma_rows(int n) { return n >= 256; }
+__host__ __device__ constexpr int xrow_stage_floats(int n) { return n + 4; }  // (n/2 + 2) complex: bulk size % 16 == 0
+__host__ __device__ constexpr size_t xtma_fft_bytes(int n);
+__host__ __device__ constexpr size_t xtma_smem_bytes(int n);
+
 __host__ __device__ constexpr size_t x_smem_bytes(int n) {
   return (size_t)(n / 2 + 1) * (cx_rows(n) + 1) * sizeof(float2);
 }
 __host__ __device__ constexpr size_t line_smem_bytes(int n) {
   return (size_t)n * cline_width(n) * cline_bpc(n) * sizeof(float2);
+}
+__host__ __device__ constexpr size_t xtma_fft_bytes(int n) { return x_smem_bytes(n); }
+// two staging buffers of cx_rows(n) rows x (n + 4) floats, the FFT buffer, two mbarriers
+__host__ __device__ constexpr size_t xtma_smem_bytes(int n) {
+  return 2 * (size_t)cx_rows(n) * xrow_stage_floats(n) * sizeof(float) + xtma_fft_bytes(n) + 64;
 }
 
 // ---------------------------------------------------------------------------------
@@ -292,21 +314,309 @@ __global__ void __launch_bounds__(SP_NT) k_z_green(const Sim* __restrict__ sims,
 }
 
 // ---------------------------------------------------------------------------------
+// TMA-streamed line pass (y forward / y inverse / z Green), one simulation per launch.
+//
+// Persistent CTA with a 3-stage shared-memory ring.  One elected thread issues the TMA
+// load of bundle i+1 while all threads transform bundle i; finished bundles leave by TMA
+// bulk store, and a stage is refilled only once the store issued from it two iterations
+// earlier has finished reading it.  A bundle is BW consecutive kx of one plane, loaded as
+// n / 256 boxes of {2 BW floats, 256 rows}.
+// ---------------------------------------------------------------------------------
+template <int N, int MODE>  // MODE 0: y forward, 1: y inverse, 2: z Green, 3: z Green (caller table)
+__global__ void __launch_bounds__(TMA_NT, 1) k_line_tma(const __grid_constant__ CUtensorMap tm,
+                                                        const Sim* __restrict__ sims, int sim_index, int nunits,
+                                                        int* err) {
+  constexpr int BW = cline_width(N), NL = BW;
+  constexpr int BOX = 256, NBOX = N / BOX;
+  constexpr int NBP = cbundles_per_plane(N), W = chalf(N);
+  constexpr unsigned STAGE = (unsigned)tma_stage_bytes(N);
+  constexpr bool ZAX = MODE >= 2;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float2* stg0 = reinterpret_cast<float2*>(smem_raw);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + TMA_STAGES * STAGE);
+  const Sim& S = sims[sim_index];
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < TMA_STAGES; ++i) mbar_init(&bar[i], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto stage_ptr = [&](int st) { return stg0 + (size_t)st * (STAGE / sizeof(float2)); };
+  auto coords = [&](int unit, int b, int& c0, int& c1, int& c2) {
+    const int plane = unit / NBP, kx0 = (unit % NBP) * BW;
+    c0 = 2 * kx0;
+    c1 = ZAX ? plane : b * BOX;
+    c2 = ZAX ? b * BOX : plane;
+  };
+  auto issue_load = [&](int unit, int st) {
+    mbar_expect_tx(&bar[st], STAGE);
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b) {
+      int c0, c1, c2;
+      coords(unit, b, c0, c1, c2);
+      tma_load_3d(stage_ptr(st) + b * BOX * BW, &tm, c0, c1, c2, &bar[st]);
+    }
+  };
+  int unit = blockIdx.x;
+  if (threadIdx.x == 0 && unit < nunits) issue_load(unit, 0);
+  unsigned parity = 0;  // bit st: parity of the next phase of stage st
+  for (int it = 0; unit < nunits; unit += gridDim.x, ++it) {
+    const int st = it % TMA_STAGES;
+    const int next = unit + gridDim.x;
+    if (threadIdx.x == 0 && next < nunits) {
+      bulk_wait_read<TMA_STAGES - 2>();  // the store that last read stage (it+1)%3 is done
+      issue_load(next, (it + 1) % TMA_STAGES);
+    }
+    const bool ok = mbar_wait(&bar[st], (parity >> st) & 1u);
+    parity ^= 1u << st;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) set_error(err, ERR_TIMEOUT);
+      break;
+    }
+    float2* s = stage_ptr(st);
+    if (MODE == 0) {
+      fft_lines<N, NL, NL, TMA_NT, false>(s, S.tw, 1);
+    } else if (MODE == 1) {
+      fft_lines<N, NL, NL, TMA_NT, true>(s, S.tw, 1);
+    } else {
+      fft_lines<N, NL, NL, TMA_NT, false>(s, S.tw, 1);
+      const float g0 = S.green;
+      const int ky = unit / NBP, kxb = (unit % NBP) * BW;
+      for (int e = threadIdx.x; e < N * NL; e += TMA_NT) {
+        const int kz = e / NL, kx = kxb + e % NL;
+        float g = 0.f;
+        if (kx < W) {
+          if (MODE == 3) {
+            g = g0 * __ldg(&S.fgrid[((long long)kz * N + ky) * N + kx]);
+          } else if ((kx | ky | kz) != 0) {
+            g = __fdividef(g0, __ldg(&S.s2[kx]) + __ldg(&S.s2[ky]) + __ldg(&S.s2[kz]));
+          }
+        }
+        const float2 v = s[e];
+        s[e] = make_float2(v.x * g, v.y * g);
+      }
+      __syncthreads();
+      fft_lines<N, NL, NL, TMA_NT, true>(s, S.tw, 1);
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int b = 0; b < NBOX; ++b) {
+        int c0, c1, c2;
+        coords(unit, b, c0, c1, c2);
+        tma_store_3d(&tm, c0, c1, c2, s + b * BOX * BW);
+      }
+      bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) bulk_wait<0>();
+}
+
+// ---------------------------------------------------------------------------------
+// x passes fed by bulk copies, one simulation per launch.
+//
+// Persistent CTA with two staging buffers.  The NR rows of a unit stream into a staging
+// buffer (one 1-D bulk copy per row, completing on an mbarrier); unit i is transposed out
+// of its buffer into the padded line-interleaved FFT buffer, the buffer is refilled at
+// once with unit i+2, and the transform and its coalesced global stores follow.
+// ---------------------------------------------------------------------------------
+template <int N, bool C2R>
+__global__ void __launch_bounds__(TMA_NT, 1) k_x_tma(const Sim* __restrict__ sims, int sim_index, int nunits,
+                                                     int* err) {
+  constexpr int M = N / 2, NR = cx_rows(N), LS = NR + 1, RS = xrow_stage_floats(N);
+  constexpr int NT = TMA_NT;
+  // bytes copied per row: R2C reads n floats; C2R reads M + 2 complex (= RS floats)
+  constexpr unsigned ROWB = C2R ? RS * 4u : N * 4u;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float* stage[2] = {reinterpret_cast<float*>(smem_raw),
+                     reinterpret_cast<float*>(smem_raw + (size_t)NR * RS * sizeof(float))};
+  float2* F = reinterpret_cast<float2*>(smem_raw + 2 * (size_t)NR * RS * sizeof(float));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + 2 * (size_t)NR * RS * sizeof(float) + xtma_fft_bytes(N));
+  const Sim& S = sims[sim_index];
+  const long long nrows = (long long)N * N;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  // warp 0 issues the copies of one unit: lane r copies rows r, r + 32, ...
+  auto issue = [&](int unit, int st) {
+    const long long row0 = (long long)unit * NR;
+    const int rows = (int)(nrows - row0 < NR ? nrows - row0 : NR);
+    if (lane == 0) mbar_expect_tx(&bar[st], (unsigned)rows * ROWB);
+    __syncwarp();
+    for (int r = lane; r < rows; r += 32) {
+      const void* src = C2R ? (const void*)(S.spec + (row0 + r) * S.pitch) : (const void*)(S.rho + (row0 + r) * N);
+      bulk_load(stage[st] + r * RS, src, ROWB, &bar[st]);
+    }
+  };
+  int unit = blockIdx.x;
+  if (warp == 0) {
+    if (unit < nunits) issue(unit, 0);
+    if (unit + (int)gridDim.x < nunits) issue(unit + gridDim.x, 1);
+  }
+  unsigned parity = 0;
+  for (int it = 0; unit < nunits; unit += gridDim.x, ++it) {
+    const int st = it & 1;
+    const long long row0 = (long long)unit * NR;
+    const bool ok = mbar_wait(&bar[st], (parity >> st) & 1u);
+    parity ^= 1u << st;
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) set_error(err, ERR_TIMEOUT);
+      break;
+    }
+    const float2* sg = reinterpret_cast<const float2*>(stage[st]);
+    if (!C2R) {
+      // z[j] = x[2j] + i x[2j+1]: staged row r, complex j -> F[j][r]
+      for (int u = threadIdx.x; u < NR * M; u += NT) {
+        const int r = u / M, j = u % M;
+        F[j * LS + r] = sg[r * (RS / 2) + j];
+      }
+    } else {
+      // tangle: Z[k] = (X[k] + X*[M-k]) + i W^-k (X[k] - X*[M-k]), pairs (k, M-k)
+      for (int u = threadIdx.x; u < NR * (M / 2 + 1); u += NT) {
+        const int r = u / (M / 2 + 1), k = u % (M / 2 + 1);
+        const float2 xk = sg[r * (RS / 2) + k];
+        const float2 xm = sg[r * (RS / 2) + (M - k)];
+        const float2 a = cadd(xk, conjf2(xm));
+        const float2 b = csub(xk, conjf2(xm));
+        const float2 w = __ldg(&S.tw[k]);
+        const float2 t = cmul(conjf2(w), b);
+        F[k * LS + r] = make_float2(a.x - t.y, a.y + t.x);
+        if (k != 0 && 2 * k != M) {
+          const float2 t2 = cmul(w, conjf2(b));
+          F[(M - k) * LS + r] = make_float2(a.x - t2.y, -a.y + t2.x);
+        }
+      }
+    }
+    __syncthreads();  // staging buffer st is free again: refill it with the unit after next
+    const int after = unit + 2 * (int)gridDim.x;
+    if (warp == 0 && after < nunits) issue(after, st);
+    fft_lines<M, NR, LS, NT, C2R>(F, S.tw, 2);
+    if (!C2R) {
+      float2* __restrict__ dst = S.spec;
+      const int P = S.pitch;
+      for (int u = threadIdx.x; u < NR * (M + 1); u += NT) {
+        const int r = u / (M + 1), k = u % (M + 1);
+        if (row0 + r >= nrows) continue;
+        const float2 zk = F[(k == M ? 0 : k) * LS + r];
+        const float2 zc = conjf2(F[(k == 0 ? 0 : M - k) * LS + r]);
+        const float2 e = cscale(cadd(zk, zc), 0.5f);
+        const float2 o = cscale(mul_mi<false>(csub(zk, zc)), 0.5f);
+        dst[(row0 + r) * P + k] = cadd(e, cmul(__ldg(&S.tw[k]), o));
+      }
+    } else {
+      float2* __restrict__ dst = reinterpret_cast<float2*>(S.phi);
+      for (int u = threadIdx.x; u < NR * M; u += NT) {
+        const int r = u / M, j = u % M;
+        if (row0 + r < nrows) dst[(row0 + r) * M + j] = F[j * LS + r];
+      }
+    }
+    __syncthreads();  // F is rewritten by the next unit
+  }
+}
+
+// Tensor map of a half spectrum seen as float32 [z][y][2*pitch], box {2 BW, 256, 1} for the
+// y pass and {2 BW, 1, 256} for the z pass.
+inline bool encode_spectrum_map(CUtensorMap* tm, const void* spec, int n, bool zaxis) {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+      return false;
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  const cuuint64_t row = (cuuint64_t)2 * cpitch(n);
+  cuuint64_t dims[3] = {row, (cuuint64_t)n, (cuuint64_t)n};
+  cuuint64_t strides[2] = {row * 4, row * 4 * (cuuint64_t)n};
+  cuuint32_t box[3] = {(cuuint32_t)(2 * cline_width(n)), zaxis ? 1u : 256u, zaxis ? 256u : 1u};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(spec), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+inline int device_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
+// ---------------------------------------------------------------------------------
 // per-N launcher (explicitly instantiated once per N in pm_spectral_n.cu)
 // ---------------------------------------------------------------------------------
+template <typename K>
+static cudaError_t max_shared(K kern, size_t bytes) {
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (!e) e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  return e;
+}
+
 template <int N>
-cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cudaStream_t st) {
+cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cudaStream_t st,
+                            const void* spec_single, int sim_index, int* err) {
   static bool init = false;
   const size_t xs = x_smem_bytes(N), ls = line_smem_bytes(N);
   if (!init) {
-    cudaError_t e = cudaFuncSetAttribute(k_x_r2c<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs);
-    if (!e) e = cudaFuncSetAttribute(k_x_c2r<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs);
-    if (!e) e = cudaFuncSetAttribute(k_y_pass<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls);
-    if (!e) e = cudaFuncSetAttribute(k_y_pass<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls);
-    if (!e) e = cudaFuncSetAttribute(k_z_green<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls);
-    if (!e) e = cudaFuncSetAttribute(k_z_green<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls);
+    if constexpr (tma_rows(N)) {
+      cudaError_t e = max_shared(k_x_tma<N, false>, xtma_smem_bytes(N));
+      if (!e) e = max_shared(k_x_tma<N, true>, xtma_smem_bytes(N));
+      if (e) return e;
+    }
+    if constexpr (tma_lines(N)) {
+      cudaError_t e = max_shared(k_line_tma<N, 0>, tma_smem_bytes(N));
+      if (!e) e = max_shared(k_line_tma<N, 1>, tma_smem_bytes(N));
+      if (!e) e = max_shared(k_line_tma<N, 2>, tma_smem_bytes(N));
+      if (!e) e = max_shared(k_line_tma<N, 3>, tma_smem_bytes(N));
+      if (e) return e;
+    }
+    cudaError_t e = max_shared(k_x_r2c<N>, xs);
+    if (!e) e = max_shared(k_x_c2r<N>, xs);
+    if (!e) e = max_shared(k_y_pass<N, false>, ls);
+    if (!e) e = max_shared(k_y_pass<N, true>, ls);
+    if (!e) e = max_shared(k_z_green<N, false>, ls);
+    if (!e) e = max_shared(k_z_green<N, true>, ls);
     if (e) return e;
     init = true;
+  }
+  if constexpr (tma_rows(N)) {
+    if (spec_single && (kind == SPEC_X_R2C || kind == SPEC_X_C2R)) {
+      const int units = (int)(((long long)N * N + cx_rows(N) - 1) / cx_rows(N));
+      const int grid = units < device_sms() ? units : device_sms();
+      if (kind == SPEC_X_R2C)
+        k_x_tma<N, false><<<grid, TMA_NT, xtma_smem_bytes(N), st>>>(sims, sim_index, units, err);
+      else
+        k_x_tma<N, true><<<grid, TMA_NT, xtma_smem_bytes(N), st>>>(sims, sim_index, units, err);
+      return cudaGetLastError();
+    }
+  }
+  if constexpr (tma_lines(N)) {
+    if (spec_single && kind != SPEC_PREPARE && kind != SPEC_X_R2C && kind != SPEC_X_C2R) {
+      const bool zax = (kind == SPEC_Z_GREEN || kind == SPEC_Z_TABLE);
+      CUtensorMap tm;
+      if (!encode_spectrum_map(&tm, spec_single, N, zax)) return cudaErrorInvalidValue;
+      const int units = N * cbundles_per_plane(N);
+      const int grid = units < device_sms() ? units : device_sms();
+      const size_t sm = tma_smem_bytes(N);
+      switch (kind) {
+        case SPEC_Y_FWD: k_line_tma<N, 0><<<grid, TMA_NT, sm, st>>>(tm, sims, sim_index, units, err); break;
+        case SPEC_Y_INV: k_line_tma<N, 1><<<grid, TMA_NT, sm, st>>>(tm, sims, sim_index, units, err); break;
+        case SPEC_Z_GREEN: k_line_tma<N, 2><<<grid, TMA_NT, sm, st>>>(tm, sims, sim_index, units, err); break;
+        default: k_line_tma<N, 3><<<grid, TMA_NT, sm, st>>>(tm, sims, sim_index, units, err); break;
+      }
+      return cudaGetLastError();
+    }
   }
   switch (kind) {
     case SPEC_PREPARE: return cudaSuccess;

@@ -6,7 +6,7 @@ namespace pm {
 
 #define PM_FOR_EACH_N(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768) X(1024)
 
-#define PM_EXTERN(NN) extern template cudaError_t spectral_launch<NN>(SpecKind, const Sim*, Work, int, cudaStream_t);
+#define PM_EXTERN(NN) extern template cudaError_t spectral_launch<NN>(SpecKind, const Sim*, Work, int, cudaStream_t, const void*, int, int*);
 PM_FOR_EACH_N(PM_EXTERN)
 #undef PM_EXTERN
 
@@ -35,9 +35,10 @@ int spectral_ctas_per_sm(SpecKind kind, int n) {
   return by_smem > 4 ? 4 : by_smem;
 }
 
-cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int ctas, cudaStream_t st) {
+cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int ctas, cudaStream_t st,
+                              const void* spec_single, int sim_index, int* err) {
   switch (n) {
-#define PM_CASE(NN) case NN: return spectral_launch<NN>(kind, sims, w, ctas, st);
+#define PM_CASE(NN) case NN: return spectral_launch<NN>(kind, sims, w, ctas, st, spec_single, sim_index, err);
     PM_FOR_EACH_N(PM_CASE)
 #undef PM_CASE
     default: return cudaErrorInvalidValue;

@@ -6,5 +6,5 @@
 #endif
 
 namespace pm {
-template cudaError_t spectral_launch<PM_N>(SpecKind, const Sim*, Work, int, cudaStream_t);
+template cudaError_t spectral_launch<PM_N>(SpecKind, const Sim*, Work, int, cudaStream_t, const void*, int, int*);
 }
