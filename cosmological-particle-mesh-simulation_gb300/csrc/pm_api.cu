@@ -67,7 +67,7 @@ Sim base_sim(pm_ctx* c, long long np) {
 void set_prefix(Call& k, long long np, int n) {
   k.prefix[PH_KEYS][1] = (int)((np + 255) / 256);
   k.prefix[PH_DEP][1] = (n / TILE_Y) * (n / TILE_Z);
-  k.prefix[PH_KICK][1] = (int)((np + 255) / 256);
+  k.prefix[PH_KICK][1] = (int)((np + KICK_UNIT - 1) / KICK_UNIT);
   k.prefix[PH_X][1] = (int)spectral_units(SPEC_X_R2C, n);
   k.prefix[PH_LINE][1] = (int)spectral_units(SPEC_Y_FWD, n);
 }
@@ -136,13 +136,13 @@ int deposit(pm_ctx* c, Call& k, unsigned* perm, unsigned* skeys, cudaStream_t st
   return PM_OK;
 }
 
-int spectral(pm_ctx* c, Call& k, bool table, cudaStream_t st) {
+int spectral(pm_ctx* c, Call& k, bool table, cudaStream_t st, bool skip_r2c = false) {
   const Sim* ds = c->d_sim.as<Sim>();
   const int n = c->n;
   const int gx = grid_for(k.prefix[PH_X][1], c->sms, 8), gl = grid_for(k.prefix[PH_LINE][1], c->sms, 8);
   const void* sp = k.sim.spec;
   int* err = c->d_err.as<int>();
-  PM_CK(spectral_dispatch(SPEC_X_R2C, n, ds, work(c, k, PH_X), gx, st, sp, 0, err), "x r2c");
+  if (!skip_r2c) PM_CK(spectral_dispatch(SPEC_X_R2C, n, ds, work(c, k, PH_X), gx, st, sp, 0, err), "x r2c");
   PM_CK(spectral_dispatch(SPEC_Y_FWD, n, ds, work(c, k, PH_LINE), gl, st, sp, 0, err), "y fwd");
   PM_CK(spectral_dispatch(table ? SPEC_Z_TABLE : SPEC_Z_GREEN, n, ds, work(c, k, PH_LINE), gl, st, sp, 0, err),
         "z green");
@@ -346,6 +346,18 @@ int pm_step(pm_ctx* c, float* positions, float* velocities, long long np, double
   if (int r = upload(c, k, st)) return r;
   unsigned *perm = nullptr, *skeys = nullptr;
   if (int r = sort_particles(c, k, st, &perm, &skeys)) return r;
+  if (!rho_out && deposit_r2c_supported(c->n)) {
+    // the density is not requested: deposit straight into the x-transformed spectrum
+    const long long nrows = (long long)c->n * c->n;
+    PM_CK(c->row_start.ensure((nrows + 1) * sizeof(unsigned)), "alloc rows");
+    PM_CK(launch_row_start(skeys, np, k.sim.xbits, (unsigned)nrows, c->row_start.as<unsigned>(), st), "rows");
+    PM_CK(deposit_r2c_dispatch(c->n, c->d_sim.as<Sim>(), work(c, k, PH_DEP), k.parts, perm,
+                               c->row_start.as<unsigned>(), POS_ABS, c->d_err.as<int>(),
+                               grid_for(k.prefix[PH_DEP][1], c->sms, 4), st),
+          "fused deposit");
+    if (int r = spectral(c, k, false, st, true)) return r;
+    return kick(c, k, perm, st);
+  }
   if (int r = deposit(c, k, perm, skeys, st)) return r;
   if (int r = spectral(c, k, false, st)) return r;
   return kick(c, k, perm, st);

@@ -45,6 +45,7 @@ struct Plan {
   int fixed_total[PH_FIXED]{};
   std::vector<int> x_total, line_total;  // per distinct size
   std::vector<int> single;               // per distinct size: the only simulation of that size, or -1
+  std::vector<int> fused, fdep_total;    // per distinct size: deposit fused with the x R2C, its tiles
   int max_dep_smem = 0;
 };
 
@@ -198,7 +199,13 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   P.bits = ceil_log2((long long)rows) + P.xbits;
   if (P.bits > 32) return bfail(b, PM_ERR_ADMIT, "batch key space exceeds 32 bits");
   std::sort(P.sizes.begin(), P.sizes.end());
-  const int nph = PH_FIXED + 2 * (int)P.sizes.size();
+  const int nph = PH_FIXED + 3 * (int)P.sizes.size();
+  for (int n : P.sizes) {
+    bool f = deposit_r2c_supported(n);
+    for (auto& sp : b->sims)
+      if (sp->n == n && (sp->cfg.flags & PM_FLAG_KEEP_DENSITY)) f = false;
+    P.fused.push_back(f ? 1 : 0);
+  }
   pre.assign((size_t)nph * (S + 1), 0);
   auto at = [&](int ph, int s) -> int& { return pre[(size_t)ph * (S + 1) + s]; };
   for (int i = 0; i < S; ++i) {
@@ -234,21 +241,27 @@ int build_plan(pm_batch* b, cudaStream_t st) {
     d.nsteps = r.nsteps;
     d.active = 1;
     d.fix_f = (r.cfg.flags & PM_FLAG_FIX_COSMO_F) ? 1 : 0;
+    const int tiles = (r.n / TILE_Y) * (r.n / TILE_Z);
+    bool fused_here = false;
+    for (size_t g = 0; g < P.sizes.size(); ++g)
+      if (P.sizes[g] == r.n) fused_here = P.fused[g] != 0;
     at(PH_KEYS, i + 1) = at(PH_KEYS, i) + (int)((r.np + 255) / 256);
-    at(PH_DEP, i + 1) = at(PH_DEP, i) + (r.n / TILE_Y) * (r.n / TILE_Z);
-    at(PH_KICK, i + 1) = at(PH_KICK, i) + (int)((r.np + 255) / 256);
+    at(PH_DEP, i + 1) = at(PH_DEP, i) + (fused_here ? 0 : tiles);
+    at(PH_KICK, i + 1) = at(PH_KICK, i) + (int)((r.np + KICK_UNIT - 1) / KICK_UNIT);
     for (size_t g = 0; g < P.sizes.size(); ++g) {
       const bool mine = P.sizes[g] == r.n;
-      const int phx = PH_FIXED + 2 * (int)g, phl = phx + 1;
+      const int phx = PH_FIXED + 3 * (int)g, phl = phx + 1, phd = phx + 2;
       at(phx, i + 1) = at(phx, i) + (mine ? (int)spectral_units(SPEC_X_R2C, r.n) : 0);
       at(phl, i + 1) = at(phl, i) + (mine ? (int)spectral_units(SPEC_Y_FWD, r.n) : 0);
+      at(phd, i + 1) = at(phd, i) + (mine && P.fused[g] ? tiles : 0);
     }
     P.max_dep_smem = std::max(P.max_dep_smem, (int)deposit_smem_bytes(r.n, TILE_Y, TILE_Z));
   }
   for (int ph = 0; ph < PH_FIXED; ++ph) P.fixed_total[ph] = at(ph, S);
   for (size_t g = 0; g < P.sizes.size(); ++g) {
-    P.x_total.push_back(at(PH_FIXED + 2 * (int)g, S));
-    P.line_total.push_back(at(PH_FIXED + 2 * (int)g + 1, S));
+    P.x_total.push_back(at(PH_FIXED + 3 * (int)g, S));
+    P.line_total.push_back(at(PH_FIXED + 3 * (int)g + 1, S));
+    P.fdep_total.push_back(at(PH_FIXED + 3 * (int)g + 2, S));
     int only = -1, count = 0;
     for (int i = 0; i < S; ++i)
       if (b->sims[i]->n == P.sizes[g]) { only = i; ++count; }
@@ -262,7 +275,12 @@ int build_plan(pm_batch* b, cudaStream_t st) {
         "upload prefix");
   PB_CK(launch_coef(b->d_sims.as<Sim>(), S, 0, st), "coef");
   PB_CK(cudaStreamSynchronize(st), "plan sync");
-  for (int n : P.sizes) PB_CK(spectral_dispatch(SPEC_PREPARE, n, nullptr, Work(), 0, st), "prepare");
+  for (size_t g = 0; g < P.sizes.size(); ++g) {
+    PB_CK(spectral_dispatch(SPEC_PREPARE, P.sizes[g], nullptr, Work(), 0, st), "prepare");
+    if (P.fused[g])
+      PB_CK(deposit_r2c_dispatch(P.sizes[g], nullptr, Work(), Parts(), nullptr, nullptr, POS_DISP, nullptr, 0, st),
+            "prepare fused deposit");
+  }
   PB_CK(deposit_prepare(), "prepare deposit");
   drop_graphs(b);
   b->dirty = false;
@@ -302,16 +320,25 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
   PB_CK(mark(1 + PP_SORT), "event");
   PB_CK(launch_row_start(skeys, P.ptot, P.xbits, P.rows, b->row_start.as<unsigned>(), st), "rows");
   PB_CK(mark(1 + PP_ROWS), "event");
-  PB_CK(launch_deposit(ds, work_of(b, PH_DEP, P.fixed_total[PH_DEP]), in, perm, b->row_start.as<unsigned>(),
-                       POS_DISP, err, grid_for(P.fixed_total[PH_DEP], b->sms, 8), P.max_dep_smem, st),
-        "deposit");
+  if (P.fixed_total[PH_DEP] > 0)
+    PB_CK(launch_deposit(ds, work_of(b, PH_DEP, P.fixed_total[PH_DEP]), in, perm, b->row_start.as<unsigned>(),
+                         POS_DISP, err, grid_for(P.fixed_total[PH_DEP], b->sms, 3), P.max_dep_smem, st),
+          "deposit");
+  for (size_t g = 0; g < P.sizes.size(); ++g) {
+    if (!P.fused[g]) continue;
+    const int tot = P.fdep_total[g];
+    PB_CK(deposit_r2c_dispatch(P.sizes[g], ds, work_of(b, PH_FIXED + 3 * (int)g + 2, tot), in, perm,
+                               b->row_start.as<unsigned>(), POS_DISP, err, grid_for(tot, b->sms, 4), st),
+          "fused deposit");
+  }
   PB_CK(mark(1 + PP_DEPOSIT), "event");
   const SpecKind order[5] = {SPEC_X_R2C, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Y_INV, SPEC_X_C2R};
   for (int o = 0; o < 5; ++o) {
     const SpecKind k = order[o];
     for (size_t g = 0; g < P.sizes.size(); ++g) {
+      if (k == SPEC_X_R2C && P.fused[g]) continue;
       const bool xk = (k == SPEC_X_R2C || k == SPEC_X_C2R);
-      const int ph = PH_FIXED + 2 * (int)g + (xk ? 0 : 1);
+      const int ph = PH_FIXED + 3 * (int)g + (xk ? 0 : 1);
       const int tot = xk ? P.x_total[g] : P.line_total[g];
       const int one = P.single[g];
       const void* sp = one >= 0 ? b->sims[one]->spec.p : nullptr;
@@ -334,7 +361,8 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
 int launches_per_step(pm_batch* b) {
   const Plan& P = b->plan;
   const int passes = radix_sort_passes(P.bits - P.xbits);
-  return 3 * passes + 1 + 1 + 5 * (int)P.sizes.size() + 1 + 1;
+  int n = 3 * passes + 1 + (P.fixed_total[PH_DEP] > 0 ? 1 : 0) + 5 * (int)P.sizes.size() + 1 + 1;
+  return n;  // each fused size replaces its x R2C launch by the fused deposit
 }
 
 int ensure_keys(pm_batch* b, cudaStream_t st) {

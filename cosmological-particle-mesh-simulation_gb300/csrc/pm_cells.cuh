@@ -1,0 +1,111 @@
+// Particle cells, CIC weights and cell keys, shared by the particle kernels and the fused
+// deposit + x-transform kernel.
+//
+// Cell key = (global x-row number << xbits) | x, where x-rows are numbered in
+// deposit-tile order (a tile is TZ planes x TY rows of full x-rows, TY = TZ = 4).
+// Sorting by key groups particles by tile and, inside a tile, by cell.
+//
+// Resident (displacement) particles carry their Lagrangian lattice index packed as
+// ix << 20 | iy << 10 | iz (N_PARTS <= 1024), so no division is needed to find q.
+#pragma once
+#include "pm_common.cuh"
+
+namespace pm {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int TY = 4, TZ = 4, NSRC = (TY + 1) * (TZ + 1);
+
+__host__ __device__ __forceinline__ unsigned pack_lattice(unsigned ix, unsigned iy, unsigned iz) {
+  return (ix << 20) | (iy << 10) | iz;
+}
+
+// ---------------------------------------------------------------------------------
+// cells
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned row_number(int y, int z, int n) {
+  const unsigned tile = (unsigned)(z / TZ) * (unsigned)(n / TY) + (unsigned)(y / TY);
+  return tile * (unsigned)(TZ * TY) + (unsigned)((z % TZ) * TY + (y % TY));
+}
+
+// Q4: a float32 coordinate equal to n (or slightly negative) is mapped into [0, n).
+__device__ __forceinline__ float canon(float x, float fn) {
+  if (x >= fn) x -= fn;
+  if (x < 0.f) x += fn;
+  if (x >= fn) x = 0.f;  // -tiny + n rounds to n
+  return x;
+}
+
+struct Cell {
+  int x, y, z;       // base cell
+  float fx, fy, fz;  // offsets in [0, 1)
+  bool ok;
+};
+
+// absolute position -> cell (density.py:19-26 with positions canonicalised)
+__device__ __forceinline__ Cell cell_abs(float x, float y, float z, int n) {
+  const float fn = (float)n;
+  Cell c;
+  x = canon(x, fn); y = canon(y, fn); z = canon(z, fn);
+  const float lx = floorf(x), ly = floorf(y), lz = floorf(z);
+  c.x = (int)lx; c.y = (int)ly; c.z = (int)lz;
+  c.fx = x - lx; c.fy = y - ly; c.fz = z - lz;
+  c.ok = isfinite(x) && isfinite(y) && isfinite(z) && c.x >= 0 && c.x < n && c.y >= 0 && c.y < n &&
+         c.z >= 0 && c.z < n;
+  return c;
+}
+
+__device__ __forceinline__ int wrap_int(int c, int n) {
+  if ((unsigned)c < (unsigned)n) return c;
+  if (c >= n && c < 2 * n) return c - n;
+  if (c < 0 && c >= -n) return c + n;
+  c %= n;
+  return c < 0 ? c + n : c;
+}
+
+// displacement from the Lagrangian lattice point -> cell:
+//   cell = (q_int + floor(q_frac + d)) mod n,  offset = (q_frac + d) - floor(q_frac + d)
+__device__ __forceinline__ Cell cell_disp(const Sim& S, unsigned id, float dx, float dy, float dz) {
+  const unsigned ix = id >> 20, iy = (id >> 10) & 1023u, iz = id & 1023u;
+  const float sx = __ldg(&S.q_frac[ix]) + dx;
+  const float sy = __ldg(&S.q_frac[iy]) + dy;
+  const float sz = __ldg(&S.q_frac[iz]) + dz;
+  const float lx = floorf(sx), ly = floorf(sy), lz = floorf(sz);
+  Cell c;
+  c.ok = isfinite(sx) && isfinite(sy) && isfinite(sz) && fabsf(lx) < 1e8f && fabsf(ly) < 1e8f &&
+         fabsf(lz) < 1e8f;
+  const int n = S.n;
+  c.x = c.ok ? wrap_int(__ldg(&S.q_int[ix]) + (int)lx, n) : 0;
+  c.y = c.ok ? wrap_int(__ldg(&S.q_int[iy]) + (int)ly, n) : 0;
+  c.z = c.ok ? wrap_int(__ldg(&S.q_int[iz]) + (int)lz, n) : 0;
+  c.fx = sx - lx; c.fy = sy - ly; c.fz = sz - lz;
+  return c;
+}
+
+template <int MODE>
+__device__ __forceinline__ Cell particle_cell(const Sim& S, const Parts& p, long long slot) {
+  if (MODE == POS_ABS) return cell_abs(p.x[slot], p.y[slot], p.z[slot], S.n);
+  return cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
+}
+
+__device__ __forceinline__ unsigned cell_key(const Sim& S, const Cell& c) {
+  return ((S.row_base + row_number(c.y, c.z, S.n)) << S.xbits) | (unsigned)c.x;
+}
+
+// The 8 CIC weights in the order of integrate.py:44-51: [ttt, dtt, tdt, ttd, ddt, dtd, tdd, ddd]
+__device__ __forceinline__ void cic_weights(const Cell& c, float w[8]) {
+  const float tx = 1.f - c.fx, ty = 1.f - c.fy, tz = 1.f - c.fz;
+  w[0] = tx * ty * tz;
+  w[1] = c.fx * ty * tz;
+  w[2] = tx * c.fy * tz;
+  w[3] = tx * ty * c.fz;
+  w[4] = c.fx * c.fy * tz;
+  w[5] = c.fx * ty * c.fz;
+  w[6] = tx * c.fy * c.fz;
+  w[7] = c.fx * c.fy * c.fz;
+}
+// corner offsets (ox, oy, oz) of the weights above
+__host__ __device__ constexpr int corner_x(int k) { return k == 1 || k == 4 || k == 5 || k == 7; }
+__host__ __device__ constexpr int corner_y(int k) { return k == 2 || k == 4 || k == 6 || k == 7; }
+__host__ __device__ constexpr int corner_z(int k) { return k == 3 || k == 5 || k == 6 || k == 7; }
+
+}  // namespace pm

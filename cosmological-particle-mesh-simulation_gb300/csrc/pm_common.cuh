@@ -106,6 +106,13 @@ int spectral_ctas_per_sm(SpecKind kind, int n);
 cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int ctas, cudaStream_t st,
                               const void* spec_single = nullptr, int sim_index = 0, int* err = nullptr);
 cudaError_t launch_fourier_grid(const Sim* sims, int ctas, cudaStream_t st);
+// fused deposit + x R2C (the density grid is not written); ctas <= 0 only prepares
+template <int N>
+cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned* perm, const unsigned* row_start,
+                               int mode, int* err, int ctas, cudaStream_t st);
+bool deposit_r2c_supported(int n);
+cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const unsigned* perm,
+                                 const unsigned* row_start, int mode, int* err, int ctas, cudaStream_t st);
 
 // particle kernels
 cudaError_t launch_keys_abs(const Sim* sims, const Work& w, Parts p, unsigned* keys, unsigned* vals,
@@ -117,6 +124,7 @@ cudaError_t launch_row_start(const unsigned* keys, long long n, int xbits, unsig
 cudaError_t launch_deposit(const Sim* sims, const Work& w, Parts p, const unsigned* perm,
                            const unsigned* row_start, int mode, int* err, int ctas, size_t smem,
                            cudaStream_t st);
+constexpr int KICK_UNIT = 512;  // particles per work unit of the kick
 cudaError_t launch_kick(const Sim* sims, const Work& w, Parts in, Parts out, const unsigned* perm,
                         unsigned* keys_next, int mode, int* err, int ctas, cudaStream_t st);
 cudaError_t launch_coef(Sim* sims, int nsims, int advance, cudaStream_t st);

@@ -8,113 +8,16 @@
 //   coef     per-step coefficients from the scale factor, in fp64 (integrate.py:11-13,
 //            potential.py:15, cosmology.py:20-27)
 //
-// Cell key = (global x-row number << xbits) | x, where x-rows are numbered in
-// deposit-tile order (a tile is TZ planes x TY rows of full x-rows, TY = TZ = 4).
-// Sorting by key groups particles by tile and, inside a tile, by cell.
-//
-// Resident (displacement) particles carry their Lagrangian lattice index packed as
-// ix << 20 | iy << 10 | iz (N_PARTS <= 1024), so no division is needed to find q.
-#include "pm_common.cuh"
+// Cells, weights and keys are defined in pm_cells.cuh, the deposit's accumulation in
+// pm_deposit.cuh (shared with the fused deposit + x-transform kernel).
+#include "pm_cells.cuh"
+#include "pm_deposit.cuh"
 
 namespace pm {
 
-constexpr int DEP_NT = 256;
 constexpr int KICK_NT = 256;
+constexpr int KICK_PPT = KICK_UNIT / KICK_NT;  // particles per thread of the kick
 constexpr int KEY_NT = 256;
-constexpr unsigned FULL = 0xffffffffu;
-constexpr int TY = 4, TZ = 4, NSRC = (TY + 1) * (TZ + 1);
-
-__host__ __device__ __forceinline__ unsigned pack_lattice(unsigned ix, unsigned iy, unsigned iz) {
-  return (ix << 20) | (iy << 10) | iz;
-}
-
-// ---------------------------------------------------------------------------------
-// cells
-// ---------------------------------------------------------------------------------
-__device__ __forceinline__ unsigned row_number(int y, int z, int n) {
-  const unsigned tile = (unsigned)(z / TZ) * (unsigned)(n / TY) + (unsigned)(y / TY);
-  return tile * (unsigned)(TZ * TY) + (unsigned)((z % TZ) * TY + (y % TY));
-}
-
-// Q4: a float32 coordinate equal to n (or slightly negative) is mapped into [0, n).
-__device__ __forceinline__ float canon(float x, float fn) {
-  if (x >= fn) x -= fn;
-  if (x < 0.f) x += fn;
-  if (x >= fn) x = 0.f;  // -tiny + n rounds to n
-  return x;
-}
-
-struct Cell {
-  int x, y, z;       // base cell
-  float fx, fy, fz;  // offsets in [0, 1)
-  bool ok;
-};
-
-// absolute position -> cell (density.py:19-26 with positions canonicalised)
-__device__ __forceinline__ Cell cell_abs(float x, float y, float z, int n) {
-  const float fn = (float)n;
-  Cell c;
-  x = canon(x, fn); y = canon(y, fn); z = canon(z, fn);
-  const float lx = floorf(x), ly = floorf(y), lz = floorf(z);
-  c.x = (int)lx; c.y = (int)ly; c.z = (int)lz;
-  c.fx = x - lx; c.fy = y - ly; c.fz = z - lz;
-  c.ok = isfinite(x) && isfinite(y) && isfinite(z) && c.x >= 0 && c.x < n && c.y >= 0 && c.y < n &&
-         c.z >= 0 && c.z < n;
-  return c;
-}
-
-__device__ __forceinline__ int wrap_int(int c, int n) {
-  if ((unsigned)c < (unsigned)n) return c;
-  if (c >= n && c < 2 * n) return c - n;
-  if (c < 0 && c >= -n) return c + n;
-  c %= n;
-  return c < 0 ? c + n : c;
-}
-
-// displacement from the Lagrangian lattice point -> cell:
-//   cell = (q_int + floor(q_frac + d)) mod n,  offset = (q_frac + d) - floor(q_frac + d)
-__device__ __forceinline__ Cell cell_disp(const Sim& S, unsigned id, float dx, float dy, float dz) {
-  const unsigned ix = id >> 20, iy = (id >> 10) & 1023u, iz = id & 1023u;
-  const float sx = __ldg(&S.q_frac[ix]) + dx;
-  const float sy = __ldg(&S.q_frac[iy]) + dy;
-  const float sz = __ldg(&S.q_frac[iz]) + dz;
-  const float lx = floorf(sx), ly = floorf(sy), lz = floorf(sz);
-  Cell c;
-  c.ok = isfinite(sx) && isfinite(sy) && isfinite(sz) && fabsf(lx) < 1e8f && fabsf(ly) < 1e8f &&
-         fabsf(lz) < 1e8f;
-  const int n = S.n;
-  c.x = c.ok ? wrap_int(__ldg(&S.q_int[ix]) + (int)lx, n) : 0;
-  c.y = c.ok ? wrap_int(__ldg(&S.q_int[iy]) + (int)ly, n) : 0;
-  c.z = c.ok ? wrap_int(__ldg(&S.q_int[iz]) + (int)lz, n) : 0;
-  c.fx = sx - lx; c.fy = sy - ly; c.fz = sz - lz;
-  return c;
-}
-
-template <int MODE>
-__device__ __forceinline__ Cell particle_cell(const Sim& S, const Parts& p, long long slot) {
-  if (MODE == POS_ABS) return cell_abs(p.x[slot], p.y[slot], p.z[slot], S.n);
-  return cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
-}
-
-__device__ __forceinline__ unsigned cell_key(const Sim& S, const Cell& c) {
-  return ((S.row_base + row_number(c.y, c.z, S.n)) << S.xbits) | (unsigned)c.x;
-}
-
-// The 8 CIC weights in the order of integrate.py:44-51: [ttt, dtt, tdt, ttd, ddt, dtd, tdd, ddd]
-__device__ __forceinline__ void cic_weights(const Cell& c, float w[8]) {
-  const float tx = 1.f - c.fx, ty = 1.f - c.fy, tz = 1.f - c.fz;
-  w[0] = tx * ty * tz;
-  w[1] = c.fx * ty * tz;
-  w[2] = tx * c.fy * tz;
-  w[3] = tx * ty * c.fz;
-  w[4] = c.fx * c.fy * tz;
-  w[5] = c.fx * ty * c.fz;
-  w[6] = tx * c.fy * c.fz;
-  w[7] = c.fx * c.fy * c.fz;
-}
-// corner offsets of the weights above
-__device__ __constant__ int c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1},
-                                              {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
 
 // ---------------------------------------------------------------------------------
 // keys
@@ -152,29 +55,12 @@ __global__ void k_row_start(const unsigned* __restrict__ keys, long long n, int 
 }
 
 // ---------------------------------------------------------------------------------
-// deposit
-//
-// One CTA per deposit tile (tz x ty full x-rows).  It gathers every particle whose base
-// cell lies in the tile's source rows (the tile plus one row/plane below, periodic),
-// adds the CIC weights that land inside the tile to integer accumulators in shared
-// memory (weights quantised to 2^-26; a 32-bit low word with carry into a 32-bit high
-// word, so the sum is exact and independent of the order of the atomics), then writes
-// the tile's rows once.  Lanes that hit the same cell in one atomic instruction are
-// serialised by the hardware; their integer sum is the same in any order.
+// deposit: one CTA per tile (pm_deposit.cuh), then the tile's rows are written once
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ void acc_add(unsigned* lo, unsigned* hi, int i, unsigned q) {
-  const unsigned old = atomicAdd(&lo[i], q);
-  if (old + q < old) atomicAdd(&hi[i], 1u);
-}
-
-__device__ __forceinline__ float fixed_to_float(unsigned l, unsigned h, float scale) {
-  return (h == 0u ? __uint2float_rn(l) : __ull2float_rn(((unsigned long long)h << 32) | l)) * scale;
-}
-
 template <int MODE>
-__global__ void __launch_bounds__(DEP_NT) k_deposit(const Sim* __restrict__ sims, Work w, Parts p,
-                                                    const unsigned* __restrict__ perm,
-                                                    const unsigned* __restrict__ row_start, int* err) {
+__global__ void __launch_bounds__(DEP_NT, 3) k_deposit(const Sim* __restrict__ sims, Work w, Parts p,
+                                                       const unsigned* __restrict__ perm,
+                                                       const unsigned* __restrict__ row_start, int* err) {
   extern __shared__ uint4 acc_raw[];
   __shared__ unsigned s_begin[NSRC];
   __shared__ unsigned s_off[NSRC + 1];
@@ -186,71 +72,9 @@ __global__ void __launch_bounds__(DEP_NT) k_deposit(const Sim* __restrict__ sims
     const int n = S.n;
     const int ntile_y = n / TY;
     const int y0 = (local % ntile_y) * TY, z0 = (local / ntile_y) * TZ;
-    const int ncell = TZ * TY * n;  // a multiple of 64
     unsigned* lo = reinterpret_cast<unsigned*>(acc_raw);
-    unsigned* hi = lo + ncell;
-    for (int i = threadIdx.x; i < ncell / 2; i += DEP_NT) acc_raw[i] = make_uint4(0u, 0u, 0u, 0u);
-    if (warp == 0) {
-      // source rows (lz, ly) in [-1, TZ-1] x [-1, TY-1]: begin and an inclusive scan of counts
-      unsigned beg = 0, cnt = 0;
-      if (lane < NSRC) {
-        const int lz = lane / (TY + 1) - 1, ly = lane % (TY + 1) - 1;
-        const int z = z0 + lz < 0 ? z0 + lz + n : z0 + lz;
-        const int y = y0 + ly < 0 ? y0 + ly + n : y0 + ly;
-        const unsigned r = S.row_base + row_number(y, z, n);
-        beg = __ldg(&row_start[r]);
-        cnt = __ldg(&row_start[r + 1]) - beg;
-      }
-      unsigned incl = cnt;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += t;
-      }
-      if (lane < NSRC) {
-        s_begin[lane] = beg;
-        s_off[lane + 1] = incl;
-      }
-      if (lane == 0) s_off[0] = 0;
-    }
-    __syncthreads();
-    const unsigned total = s_off[NSRC];
-    for (unsigned base = (unsigned)warp * 32u; base < total; base += DEP_NT) {
-      const unsigned f = base + lane;
-      const bool valid = f < total;
-      float wt[8];
-      int cx = 0, ly = 0, lz = 0;
-      bool ok = false;
-      if (valid) {
-        int r = 0;  // last source row with s_off[r] <= f
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-          if (r + step < NSRC && s_off[r + step] <= f) r += step;
-        const unsigned slot = __ldg(&perm[s_begin[r] + (f - s_off[r])]);
-        const Cell c = particle_cell<MODE>(S, p, slot);
-        int dy = c.y - y0, dz = c.z - z0;
-        if (dy >= n - 1) dy -= n;
-        if (dz >= n - 1) dz -= n;
-        ok = c.ok && dy >= -1 && dy < TY && dz >= -1 && dz < TZ;
-        if (!ok) {
-          set_error(err, c.ok ? ERR_SOURCE_ROW : ERR_CELL_RANGE);
-        } else {
-          cic_weights(c, wt);
-          cx = c.x; ly = dy; lz = dz;
-        }
-      }
-      if (ok) {
-        const int x1 = cx + 1 == n ? 0 : cx + 1;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const int ty2 = ly + c_corner[k][1], tz2 = lz + c_corner[k][2];
-          if (ty2 >= 0 && ty2 < TY && tz2 >= 0 && tz2 < TZ)
-            acc_add(lo, hi, (tz2 * TY + ty2) * n + (c_corner[k][0] ? x1 : cx),
-                    __float2uint_rn(wt[k] * (float)(1u << PM_FIX_BITS)));
-        }
-      }
-    }
-    __syncthreads();
+    unsigned* hi = lo + TZ * TY * n;
+    deposit_tile<MODE, DEP_NT>(S, p, perm, row_start, err, y0, z0, lo, hi, s_begin, s_off);
     const float ms = S.mass_scale;
     for (int row = warp; row < TZ * TY; row += DEP_NT / 32) {
       const uint4* l4 = reinterpret_cast<const uint4*>(lo + row * n);
@@ -288,21 +112,26 @@ __device__ __forceinline__ void gather_force(const float* __restrict__ phi, int 
   const int ym = c.y == 0 ? n - 1 : c.y - 1, y1 = c.y + 1 == n ? 0 : c.y + 1, y2 = y1 + 1 == n ? 0 : y1 + 1;
   const int zm = c.z == 0 ? n - 1 : c.z - 1, z1 = c.z + 1 == n ? 0 : c.z + 1, z2 = z1 + 1 == n ? 0 : z1 + 1;
   const int x0 = c.x, y0 = c.y, z0 = c.z;
-  const long long nn = n;
-  auto P = [&](int x, int y, int z) { return __ldg(&phi[((long long)z * nn + y) * nn + x]); };
-  // x gradient: rows (y0|y1, z0|z1) at xm, x0, x1, x2
-  const float a00m = P(xm, y0, z0), a000 = P(x0, y0, z0), a001 = P(x1, y0, z0), a002 = P(x2, y0, z0);
-  const float a10m = P(xm, y1, z0), a100 = P(x0, y1, z0), a101 = P(x1, y1, z0), a102 = P(x2, y1, z0);
-  const float a01m = P(xm, y0, z1), a010 = P(x0, y0, z1), a011 = P(x1, y0, z1), a012 = P(x2, y0, z1);
-  const float a11m = P(xm, y1, z1), a110 = P(x0, y1, z1), a111 = P(x1, y1, z1), a112 = P(x2, y1, z1);
+  // the 12 x-rows the 32 taps lie in
+  auto row = [&](int y, int z) { return phi + (size_t)(unsigned)(z * n + y) * (unsigned)n; };
+  const float* r00 = row(y0, z0); const float* r10 = row(y1, z0);
+  const float* r01 = row(y0, z1); const float* r11 = row(y1, z1);
+  const float* rm0 = row(ym, z0); const float* rm1 = row(ym, z1);
+  const float* r20 = row(y2, z0); const float* r21 = row(y2, z1);
+  const float* r0m = row(y0, zm); const float* r1m = row(y1, zm);
+  const float* r02 = row(y0, z2); const float* r12 = row(y1, z2);
+  // x gradient taps: rows (y0|y1, z0|z1) at xm, x0, x1, x2   (naming a<y><z><x>)
+  const float a00m = __ldg(r00 + xm), a000 = __ldg(r00 + x0), a001 = __ldg(r00 + x1), a002 = __ldg(r00 + x2);
+  const float a10m = __ldg(r10 + xm), a100 = __ldg(r10 + x0), a101 = __ldg(r10 + x1), a102 = __ldg(r10 + x2);
+  const float a01m = __ldg(r01 + xm), a010 = __ldg(r01 + x0), a011 = __ldg(r01 + x1), a012 = __ldg(r01 + x2);
+  const float a11m = __ldg(r11 + xm), a110 = __ldg(r11 + x0), a111 = __ldg(r11 + x1), a112 = __ldg(r11 + x2);
   // y extension rows ym, y2 at x0, x1 (z0, z1)
-  const float bm00 = P(x0, ym, z0), bm01 = P(x1, ym, z0), b200 = P(x0, y2, z0), b201 = P(x1, y2, z0);
-  const float bm10 = P(x0, ym, z1), bm11 = P(x1, ym, z1), b210 = P(x0, y2, z1), b211 = P(x1, y2, z1);
+  const float bm00 = __ldg(rm0 + x0), bm01 = __ldg(rm0 + x1), b200 = __ldg(r20 + x0), b201 = __ldg(r20 + x1);
+  const float bm10 = __ldg(rm1 + x0), bm11 = __ldg(rm1 + x1), b210 = __ldg(r21 + x0), b211 = __ldg(r21 + x1);
   // z extension planes zm, z2 at (x0|x1, y0|y1)
-  const float cm00 = P(x0, y0, zm), cm01 = P(x1, y0, zm), cm10 = P(x0, y1, zm), cm11 = P(x1, y1, zm);
-  const float c200 = P(x0, y0, z2), c201 = P(x1, y0, z2), c210 = P(x0, y1, z2), c211 = P(x1, y1, z2);
-  // phi at corner (ox, oy, oz): a[oy][oz][ox] with a?? naming: a<y><z><x>
-  // x axis: g(o) = phi[x+ox-1] - phi[x+ox+1]
+  const float cm00 = __ldg(r0m + x0), cm01 = __ldg(r0m + x1), cm10 = __ldg(r1m + x0), cm11 = __ldg(r1m + x1);
+  const float c200 = __ldg(r02 + x0), c201 = __ldg(r02 + x1), c210 = __ldg(r12 + x0), c211 = __ldg(r12 + x1);
+  // x axis: g(o) = phi[x+ox-1] - phi[x+ox+1]   (corner naming g<ox><oy><oz>)
   const float gx000 = a00m - a001, gx100 = a000 - a002;
   const float gx010 = a10m - a101, gx110 = a100 - a102;
   const float gx001 = a01m - a011, gx101 = a010 - a012;
@@ -318,7 +147,6 @@ __device__ __forceinline__ void gather_force(const float* __restrict__ phi, int 
   const float gz001 = a000 - c200, gz101 = a001 - c201;
   const float gz011 = a100 - c210, gz111 = a101 - c211;
   // integrate.py:92 order: g*t0 + g_x*t1 + g_y*t2 + g_z*t3 + g_xy*t4 + g_xz*t5 + g_yz*t6 + g_xyz*t7
-  // corner naming g<ox><oy><oz>
   g[0] = (gx000 * w[0] + gx100 * w[1] + gx010 * w[2] + gx001 * w[3] + gx110 * w[4] + gx101 * w[5] +
           gx011 * w[6] + gx111 * w[7]) * 0.5f;
   g[1] = (gy000 * w[0] + gy100 * w[1] + gy010 * w[2] + gy001 * w[3] + gy110 * w[4] + gy101 * w[5] +
@@ -327,6 +155,42 @@ __device__ __forceinline__ void gather_force(const float* __restrict__ phi, int 
           gz011 * w[6] + gz111 * w[7]) * 0.5f;
 }
 
+// Kick/drift of one particle whose state and force are in registers; writes it out.
+template <int MODE>
+__device__ __forceinline__ void kick_store(const Sim& S, const Parts& out, long long sp, long long slot, float px,
+                                           float py, float pz, float vx, float vy, float vz, unsigned id,
+                                           const float (&g)[3], unsigned* __restrict__ keys_next, int* err) {
+  const float kk = S.kick, dr = S.drift;
+  vx = fmaf(kk, g[0], vx);
+  vy = fmaf(kk, g[1], vy);
+  vz = fmaf(kk, g[2], vz);
+  if (MODE == POS_ABS) {
+    // positions may arrive as exactly n (Q4): drift the canonical value and wrap
+    const float fn = (float)S.n;
+    const float nx = canon(fmaf(dr, vx, canon(px, fn)), fn);
+    const float ny = canon(fmaf(dr, vy, canon(py, fn)), fn);
+    const float nz = canon(fmaf(dr, vz, canon(pz, fn)), fn);
+    if (!(isfinite(nx) && isfinite(ny) && isfinite(nz) && isfinite(vx) && isfinite(vy) && isfinite(vz)))
+      set_error(err, ERR_NONFINITE);
+    out.x[slot] = nx; out.y[slot] = ny; out.z[slot] = nz;
+    out.vx[slot] = vx; out.vy[slot] = vy; out.vz[slot] = vz;
+  } else {
+    const float nx = fmaf(dr, vx, px), ny = fmaf(dr, vy, py), nz = fmaf(dr, vz, pz);
+    if (!(isfinite(nx) && isfinite(ny) && isfinite(nz) && isfinite(vx) && isfinite(vy) && isfinite(vz)))
+      set_error(err, ERR_NONFINITE);
+    out.x[sp] = nx; out.y[sp] = ny; out.z[sp] = nz;
+    out.vx[sp] = vx; out.vy[sp] = vy; out.vz[sp] = vz;
+    out.id[sp] = id;
+    if (keys_next) {
+      Cell cn = cell_disp(S, id, nx, ny, nz);
+      if (!cn.ok) { set_error(err, ERR_CELL_RANGE); cn.x = cn.y = cn.z = 0; }
+      keys_next[sp] = cell_key(S, cn);
+    }
+  }
+}
+
+// Each thread advances KICK_PPT particles, KICK_NT apart: all their loads (state, then the
+// 32 potential taps each) are issued before any store, so that they overlap.
 template <int MODE>
 __global__ void __launch_bounds__(KICK_NT) k_kick(const Sim* __restrict__ sims, Work w, Parts in, Parts out,
                                                   const unsigned* __restrict__ perm,
@@ -334,47 +198,39 @@ __global__ void __launch_bounds__(KICK_NT) k_kick(const Sim* __restrict__ sims, 
   for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
     const int si = locate_sim(w, unit);
     const Sim& S = sims[si];
-    const long long i = (long long)(unit - __ldg(&w.prefix[si])) * KICK_NT + threadIdx.x;
-    if (i >= S.np) continue;
-    const long long sp = S.part_off + i;  // position in sorted order (or slot without perm)
-    const long long slot = perm ? (long long)__ldg(&perm[sp]) : sp;
-    const float px = in.x[slot], py = in.y[slot], pz = in.z[slot];
-    float vx = in.vx[slot], vy = in.vy[slot], vz = in.vz[slot];
-    Cell c;
-    unsigned id = 0;
-    if (MODE == POS_ABS) {
-      c = cell_abs(px, py, pz, S.n);
-    } else {
-      id = in.id[slot];
-      c = cell_disp(S, id, px, py, pz);
+    const long long i0 = (long long)(unit - __ldg(&w.prefix[si])) * (KICK_NT * KICK_PPT) + threadIdx.x;
+    long long sp[KICK_PPT], slot[KICK_PPT];
+    float px[KICK_PPT], py[KICK_PPT], pz[KICK_PPT], vx[KICK_PPT], vy[KICK_PPT], vz[KICK_PPT];
+    unsigned id[KICK_PPT];
+    Cell c[KICK_PPT];
+#pragma unroll
+    for (int q = 0; q < KICK_PPT; ++q) {
+      const long long i = i0 + q * KICK_NT;
+      sp[q] = S.part_off + i;  // position in sorted order (or slot without perm)
+      slot[q] = i < S.np ? (perm ? (long long)__ldg(&perm[sp[q]]) : sp[q]) : -1;
     }
-    float g[3] = {0.f, 0.f, 0.f};
-    if (c.ok) gather_force(S.phi, S.n, c, g);
-    else set_error(err, ERR_CELL_RANGE);
-    const float kk = S.kick, dr = S.drift;
-    vx = fmaf(kk, g[0], vx);
-    vy = fmaf(kk, g[1], vy);
-    vz = fmaf(kk, g[2], vz);
-    float nx = fmaf(dr, vx, px), ny = fmaf(dr, vy, py), nz = fmaf(dr, vz, pz);
-    if (!(isfinite(nx) && isfinite(ny) && isfinite(nz) && isfinite(vx) && isfinite(vy) && isfinite(vz)))
-      set_error(err, ERR_NONFINITE);
-    if (MODE == POS_ABS) {
-      const float fn = (float)S.n;
-      // positions may arrive as exactly n (Q4): wrap the canonical value
-      nx = canon(fmaf(dr, vx, canon(px, fn)), fn);
-      ny = canon(fmaf(dr, vy, canon(py, fn)), fn);
-      nz = canon(fmaf(dr, vz, canon(pz, fn)), fn);
-      out.x[slot] = nx; out.y[slot] = ny; out.z[slot] = nz;
-      out.vx[slot] = vx; out.vy[slot] = vy; out.vz[slot] = vz;
-    } else {
-      out.x[sp] = nx; out.y[sp] = ny; out.z[sp] = nz;
-      out.vx[sp] = vx; out.vy[sp] = vy; out.vz[sp] = vz;
-      out.id[sp] = id;
-      if (keys_next) {
-        Cell cn = cell_disp(S, id, nx, ny, nz);
-        if (!cn.ok) { set_error(err, ERR_CELL_RANGE); cn.x = cn.y = cn.z = 0; }
-        keys_next[sp] = cell_key(S, cn);
-      }
+#pragma unroll
+    for (int q = 0; q < KICK_PPT; ++q) {
+      const long long sl = slot[q] >= 0 ? slot[q] : 0;
+      px[q] = in.x[sl]; py[q] = in.y[sl]; pz[q] = in.z[sl];
+      vx[q] = in.vx[sl]; vy[q] = in.vy[sl]; vz[q] = in.vz[sl];
+      id[q] = MODE == POS_DISP ? in.id[sl] : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < KICK_PPT; ++q)
+      c[q] = MODE == POS_ABS ? cell_abs(px[q], py[q], pz[q], S.n) : cell_disp(S, id[q], px[q], py[q], pz[q]);
+    float g[KICK_PPT][3];
+#pragma unroll
+    for (int q = 0; q < KICK_PPT; ++q) {
+      g[q][0] = g[q][1] = g[q][2] = 0.f;
+      if (slot[q] >= 0 && c[q].ok) gather_force(S.phi, S.n, c[q], g[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < KICK_PPT; ++q) {
+      if (slot[q] < 0) continue;
+      if (!c[q].ok) set_error(err, ERR_CELL_RANGE);
+      kick_store<MODE>(S, out, sp[q], slot[q], px[q], py[q], pz[q], vx[q], vy[q], vz[q], id[q], g[q], keys_next,
+                       err);
     }
   }
 }

@@ -14,6 +14,7 @@
 #include <cudaTypedefs.h>
 
 #include "pm_common.cuh"
+#include "pm_deposit.cuh"
 #include "pm_fft.cuh"
 #include "pm_tma.cuh"
 
@@ -516,6 +517,93 @@ __global__ void __launch_bounds__(TMA_NT, 1) k_x_tma(const Sim* __restrict__ sim
       }
     }
     __syncthreads();  // F is rewritten by the next unit
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// fused deposit + x R2C: one CTA per deposit tile.  The tile's TZ x TY rows are deposited
+// into shared memory (pm_deposit.cuh), converted to float, transposed into the padded
+// line-interleaved FFT buffer (reusing the accumulator space) and transformed along x;
+// the half-spectrum rows are written directly, so the density grid never goes to HBM.
+// ---------------------------------------------------------------------------------
+__host__ __device__ constexpr size_t deposit_r2c_smem_bytes(int n) {
+  return (size_t)2 * TZ * TY * n * sizeof(unsigned);  // >= (n/2) * (TZ*TY + 1) * sizeof(float2)
+}
+// sizes whose tile (TZ * TY rows of n cells) divides evenly over the block
+__host__ __device__ constexpr bool deposit_r2c_ok(int n) { return (TZ * TY * n) % DEP_NT == 0; }
+
+template <int N, int MODE>
+__global__ void __launch_bounds__(DEP_NT, 2) k_deposit_r2c(const Sim* __restrict__ sims, Work w, Parts p,
+                                                           const unsigned* __restrict__ perm,
+                                                           const unsigned* __restrict__ row_start, int* err) {
+  constexpr int M = N / 2, NL = TZ * TY, LS = NL + 1;
+  constexpr int PER = NL * N / DEP_NT;
+  static_assert(NL * N % DEP_NT == 0, "tile cells must divide by the block size");
+  static_assert((size_t)M * LS * sizeof(float2) <= deposit_r2c_smem_bytes(N), "FFT buffer must fit");
+  extern __shared__ uint4 acc_raw[];
+  __shared__ unsigned s_begin[NSRC];
+  __shared__ unsigned s_off[NSRC + 1];
+  unsigned* lo = reinterpret_cast<unsigned*>(acc_raw);
+  unsigned* hi = lo + NL * N;
+  float2* F = reinterpret_cast<float2*>(acc_raw);
+  float* Ff = reinterpret_cast<float*>(acc_raw);
+  for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
+    const int si = locate_sim(w, unit);
+    const Sim& S = sims[si];
+    const int local = unit - __ldg(&w.prefix[si]);
+    const int y0 = (local % (N / TY)) * TY, z0 = (local / (N / TY)) * TZ;
+    deposit_tile<MODE, DEP_NT>(S, p, perm, row_start, err, y0, z0, lo, hi, s_begin, s_off);
+    const float ms = S.mass_scale;
+    float v[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int i = threadIdx.x + k * DEP_NT;
+      v[k] = fixed_to_float(lo[i], hi[i], ms);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int i = threadIdx.x + k * DEP_NT;
+      const int r = i / N, x = i % N;
+      Ff[((x >> 1) * LS + r) * 2 + (x & 1)] = v[k];  // z[j] = x[2j] + i x[2j+1] of row r
+    }
+    __syncthreads();
+    fft_lines<M, NL, LS, DEP_NT, false>(F, S.tw, 2);
+    float2* __restrict__ dst = S.spec;
+    const int P = S.pitch;
+    for (int u = threadIdx.x; u < NL * (M + 1); u += DEP_NT) {
+      const int r = u / (M + 1), k = u % (M + 1);
+      const long long row = (long long)(z0 + r / TY) * N + (y0 + r % TY);
+      const float2 zk = F[(k == M ? 0 : k) * LS + r];
+      const float2 zc = conjf2(F[(k == 0 ? 0 : M - k) * LS + r]);
+      const float2 e = cscale(cadd(zk, zc), 0.5f);
+      const float2 o = cscale(mul_mi<false>(csub(zk, zc)), 0.5f);
+      dst[row * P + k] = cadd(e, cmul(__ldg(&S.tw[k]), o));
+    }
+    __syncthreads();
+  }
+}
+
+template <int N>
+cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned* perm, const unsigned* row_start,
+                               int mode, int* err, int ctas, cudaStream_t st) {
+  if constexpr (!deposit_r2c_ok(N)) {
+    return cudaErrorNotSupported;
+  } else {
+  static bool init = false;
+  const size_t sm = deposit_r2c_smem_bytes(N);
+  if (!init) {
+    cudaError_t e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_ABS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (!e) e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_DISP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (!e) e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_ABS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (!e) e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_DISP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e) return e;
+    init = true;
+  }
+  if (ctas <= 0) return cudaSuccess;  // attribute setup only
+  if (mode == POS_ABS) k_deposit_r2c<N, POS_ABS><<<ctas, DEP_NT, sm, st>>>(sims, w, p, perm, row_start, err);
+  else k_deposit_r2c<N, POS_DISP><<<ctas, DEP_NT, sm, st>>>(sims, w, p, perm, row_start, err);
+  return cudaGetLastError();
   }
 }
 

@@ -9,6 +9,23 @@ namespace pm {
 #define PM_EXTERN(NN) extern template cudaError_t spectral_launch<NN>(SpecKind, const Sim*, Work, int, cudaStream_t, const void*, int, int*);
 PM_FOR_EACH_N(PM_EXTERN)
 #undef PM_EXTERN
+#define PM_EXTERN(NN)                                                                                         \
+  extern template cudaError_t deposit_r2c_launch<NN>(const Sim*, Work, Parts, const unsigned*, const unsigned*, \
+                                                     int, int*, int, cudaStream_t);
+PM_FOR_EACH_N(PM_EXTERN)
+#undef PM_EXTERN
+
+cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const unsigned* perm,
+                                 const unsigned* row_start, int mode, int* err, int ctas, cudaStream_t st) {
+  switch (n) {
+#define PM_CASE(NN) case NN: return deposit_r2c_launch<NN>(sims, w, p, perm, row_start, mode, err, ctas, st);
+    PM_FOR_EACH_N(PM_CASE)
+#undef PM_CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+bool deposit_r2c_supported(int n) { return (TZ * TY * n) % DEP_NT == 0; }
 
 bool spectral_supported(int n) {
   switch (n) {
