@@ -1,0 +1,83 @@
+"""The drop-in modules (density.py, fourier_utils.py, potential.py, integrate.py, pmesh.py)
+used exactly as the reference's driver uses its own modules, on numpy arrays."""
+import importlib
+import sys
+import types
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, periodic_maxdiff, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+DROPIN = ["configure_me", "density", "fourier_utils", "potential", "integrate", "cosmology",
+          "gaussian_random_field", "zeldovich", "save_data", "pmesh"]
+
+
+def install_config(c, **extra):
+    for m in DROPIN:
+        sys.modules.pop(m, None)
+    cm = types.ModuleType("configure_me")
+    for k, v in c.items():
+        if k.isupper():
+            setattr(cm, k, v)
+    cm.N_SAVE_FILES, cm.N_PLOTS = 10, 10
+    cm.PLOT_STEPS = cm.PLOT_PROJECTIONS = cm.PLOT_GRF = False
+    cm.SAVE_DATA = cm.SAVE_DENSITY = False
+    cm.PRINT_STATUS = False
+    cm.RESTART, cm.RESTART_FROM_N = False, 0
+    cm.RESIDENT = False
+    for k, v in extra.items():
+        setattr(cm, k, v)
+    sys.modules["configure_me"] = cm
+    return cm
+
+
+@pytest.fixture
+def restore_modules():
+    yield
+    for m in DROPIN:
+        sys.modules.pop(m, None)
+
+
+def test_reference_loop_body_on_dropin_modules(cuda, restore_modules):
+    f, c = load_golden("n16_g32")
+    install_config(c)
+    density = importlib.import_module("density")
+    fourier_utils = importlib.import_module("fourier_utils")
+    integrate = importlib.import_module("integrate")
+    potential = importlib.import_module("potential")
+    n = c["N_CELLS"]
+    mass = (n / c["N_PARTS"]) ** 3
+    da = (c["A_END"] - c["A_INIT"]) / c["STEPS"]
+    fg = fourier_utils.fourier_grid()
+    assert isinstance(fg, np.ndarray) and fg.shape == (n, n, n)
+    pos, vel = f["pos0"].copy(), f["vel0"].copy()
+    a = c["A_INIT"]
+    for s in range(c["steps"]):
+        rho = density.density(pos, mass)
+        assert isinstance(rho, np.ndarray) and rho.dtype == np.float32
+        assert rel_l2(rho, f[f"rho{s}"]) < 1e-5
+        phi = potential.potential(rho, fg, a)
+        assert rel_l2(phi, f[f"phi{s}"]) < 1e-5
+        p2, v2 = integrate.advance_time(rho, pos, vel, fg, a, da)
+        assert p2 is pos and v2 is vel  # updated in place, like the reference
+        assert rel_l2(vel, f[f"vel{s + 1}"]) < 1e-4
+        assert periodic_maxdiff(pos, f[f"pos{s + 1}"], n) < 1e-3
+        a += da
+
+
+def test_pmesh_driver_resident_and_loop_agree(cuda, restore_modules):
+    f, c = load_golden("n16_g32")
+    c = dict(c, STEPS=20)
+    results = []
+    for resident in (False, True):
+        install_config(c, RESIDENT=resident)
+        pmesh = importlib.import_module("pmesh")
+        pos, vel = pmesh.simulator()
+        results.append((np.asarray(pos), np.asarray(vel)))
+    (p0, v0), (p1, v1) = results
+    # the resident engine stores displacements (more precise): small differences only
+    assert periodic_maxdiff(p0, p1, c["N_CELLS"]) < 5e-3
+    assert rel_l2(v0, v1) < 1e-3
