@@ -45,6 +45,7 @@ SIGNATURES = {
     "pm_step_host": (c_int, [c_void_p, c_void_p, c_void_p, c_ll, c_double, c_double, c_double, c_void_p]),
     "pm_cosmo_f": (c_double, [c_double, c_double, c_double, c_double]),
     "pm_sort_keys": (c_int, [c_void_p, c_void_p, c_ll, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pm_density_noalloc": (c_int, [c_void_p, c_ll, c_int, c_double, c_void_p, c_void_p]),
     "pm_batch_create": (c_int, [c_int, c_size_t, ctypes.POINTER(c_void_p)]),
     "pm_batch_destroy": (None, [c_void_p]),
     "pm_batch_last_error": (c_char_p, [c_void_p]),

@@ -111,6 +111,17 @@ double pm_cosmo_f(double a, double om, double ol, double ok);
 int pm_sort_keys(pm_ctx* ctx, const float* positions, long long np, unsigned* keys_out,
                  unsigned* sorted_keys, unsigned* perm, void* stream);
 
+/* The CIC deposit of pm_density for callers that cannot allocate device memory (code
+   running during stream capture, memory carved up by an arena, latency-critical loops).
+   No counterpart in the reference.  All scratch lives in one static device array of the
+   library (about 4.3 MB per GPU, held until the process exits): at most 262,144
+   particles and n_cells <= 128, otherwise PM_ERR_ARG.  Calls no allocating routine.  The
+   first call on a device looks up the array's address (cudaGetSymbolAddress) and sets
+   kernel attributes: make it before any stream capture.  Calls share the array, so calls
+   that overlap on the GPU race; invalid particles are skipped without a report. */
+int pm_density_noalloc(const float* positions, long long np, int n_cells, double mass, float* rho,
+                       void* stream);
+
 /* ---- resident engine: batches of simulations ------------------------------------ */
 typedef struct pm_batch pm_batch;
 
