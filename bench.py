@@ -124,7 +124,7 @@ def measured_peak():
 def profiled_traffic():
     """Per-launch DRAM bytes (dram__bytes_read.sum + write.sum) of each phase's kernel from
     the committed ncu summary, scaled to the full workload there; None if absent."""
-    path = os.path.join(ROOT, "profiles", "traffic_cfg2.md")
+    path = os.path.join(ROOT, "profiles", "kernels_512g_full.md")
     out = {}
     try:
         for line in open(path):
@@ -141,8 +141,9 @@ def algorithmic_bytes(np_, n):
     nc = n ** 3
     h = n * n * (n // 2 + 1)
     return {
-        "deposit": 12 * np_ + 4 * nc,
-        "x_r2c": 4 * nc + 8 * h,
+        # the resident step fuses the deposit with the x R2C: particles in, spectrum rows out
+        "deposit": 12 * np_ + 8 * h,
+        "x_r2c": 0,
         "y_fwd": 16 * h,
         "z_green": 16 * h,
         "y_inv": 16 * h,
