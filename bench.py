@@ -313,6 +313,119 @@ def cpu_baseline(cfg, pos, vel, steps):
             "seconds": round(t, 2)}
 
 
+def _ics_pool(cfgs, workers=16):
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    from pmgpu import ics
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(ics.initial_conditions, cfgs))
+
+
+def batched_configs(count=64, seed=0):
+    """Ensemble of independent simulations: seeds 0..count-1, N_PARTS uniform in {32, 48, 64,
+    96, 128}, grid 2 N_PARTS, box uniform in [50, 500] Mpc/h, 200 steps each."""
+    import numpy as np
+    from pmgpu.config import Config
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(count):
+        n = int(rng.choice([32, 48, 64, 96, 128]))
+        out.append(Config(n_parts=n, n_cells=2 * n, box_size=float(rng.uniform(50.0, 500.0)), random_seed=s,
+                          steps=200))
+    return out
+
+
+def run_batched(args, local):
+    """All simulations in one batch (one launch per phase, CUDA graphs) vs each one alone."""
+    import torch
+    import pmgpu
+    from pmgpu.batch import Batch
+    from pmgpu.config import step_count
+    torch.cuda.set_device(local)
+    pmgpu.build()
+    cfgs = batched_configs(args.batch_sims)
+    ics_ = _ics_pool(cfgs)
+    steps = [step_count(c.a_init, c.a_end, c.steps) for c in cfgs]
+    pu = sum(c.np_total * k for c, k in zip(cfgs, steps))
+    warm = Batch(device=local)
+    for c, (p, v) in zip(cfgs[:8], ics_[:8]):
+        warm.add(c, p, v)
+    warm.step(2)
+    warm.close()
+    stream = torch.cuda.Stream()
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    b = Batch(device=local)
+    ids = [b.add(c, p, v) for c, (p, v) in zip(cfgs, ics_)]
+    t_batch = timed(lambda: b.step(max(steps) + 1))
+    b.check_device()
+    assert all(b.state(i)[1] == k for i, k in zip(ids, steps))
+    b.close()
+    pb = Batch(device=local)
+    for c, (p, v) in zip(cfgs, ics_):
+        pb.add(c, p, v)
+    pb.step(2)
+    prof = pb.profile(3)
+    launches = pb.launches_per_step()
+    pb.close()
+
+    def plain():
+        for c, (p, v) in zip(cfgs, ics_):
+            one = Batch(device=local)
+            one.add(c, p, v)
+            one.step(step_count(c.a_init, c.a_end, c.steps) + 1)
+            one.close()
+    t_plain = timed(plain)
+    line = {"metric": METRIC, "workload": "batched", "value": pu / t_batch, "unit": UNIT,
+            "plain_value": pu / t_plain, "batched_over_plain": t_plain / t_batch, "sims": len(cfgs),
+            "particle_updates": pu, "seconds_batched": round(t_batch, 3), "seconds_plain": round(t_plain, 3),
+            "batched_phase_ms": {k: round(v, 4) for k, v in prof.items()}, "launches_per_step": launches,
+            "dtype": "f32", "data": "synthetic: seeded GRF + Zel'dovich ICs (reference algorithm)",
+            "config": {"workload": f"{len(cfgs)} simulations, seeds 0-{len(cfgs) - 1}, N_PARTS in "
+                                   "{32,48,64,96,128}, grid 2N, box U(50,500) Mpc/h, 200 steps",
+                       "plain": "each simulation alone in its own resident batch, one after another"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_served(args, local):
+    """Poisson request stream against one GPU: continuous batching under a memory cap."""
+    import torch
+    import pmgpu
+    from pmgpu.serve import Server, poisson_stream, summarize
+    torch.cuda.set_device(local)
+    pmgpu.build()
+    stream = poisson_stream(args.serve_rate, args.serve_seconds, seed=0)
+    srv = Server(mem_cap_bytes=int(args.serve_cap_gb * 2 ** 30), ic_workers=args.ic_workers,
+                 steps_per_tick=args.steps_per_tick, device=local)
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        res = srv.run(stream)
+    wall = time.perf_counter() - t0
+    srv.close()
+    summ = summarize(res, wall)
+    offered = sum(r.particle_updates for r in stream) / args.serve_seconds
+    line = {"metric": METRIC, "workload": "served", "value": summ["particle_updates_per_s"], "unit": UNIT,
+            "p50_latency_s": summ["p50_latency_s"], "p99_latency_s": summ["p99_latency_s"],
+            "mean_latency_s": summ["mean_latency_s"], "requests": summ["requests"], "offered_requests": len(stream),
+            "offered_particle_updates_per_s": offered, "wall_s": round(wall, 2), "dtype": "f32",
+            "data": "synthetic request stream (seeded)",
+            "config": {"workload": f"Poisson {args.serve_rate} req/s for {args.serve_seconds} s, N_PARTS in "
+                                   "{64,96,128,192,256} weighted 40/25/20/10/5%, grid 2N, box U(100,500), "
+                                   "steps U(50,500)", "memory_cap_gb": args.serve_cap_gb,
+                       "steps_per_tick": args.steps_per_tick, "ic_workers": args.ic_workers},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -348,10 +461,25 @@ def main():
     ap.add_argument("--n-parts", type=int, default=256, help="reduced cases for profiling only")
     ap.add_argument("--n-cells", type=int, default=512)
     ap.add_argument("--box", type=float, default=250.0)
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served"],
+                    help="plain: the README workload (headline); batched / served: the ensemble and "
+                         "request-stream workloads")
+    ap.add_argument("--batch-sims", type=int, default=64)
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-seconds", type=float, default=120.0)
+    ap.add_argument("--serve-cap-gb", type=float, default=150.0)
+    ap.add_argument("--steps-per-tick", type=int, default=4)
+    ap.add_argument("--ic-workers", type=int, default=12)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+    elif args.workload == "batched":
+        if rank == 0:
+            run_batched(args, local)
+    elif args.workload == "served":
+        if rank == 0:
+            run_served(args, local)
     else:
         run_gpu(args, ws, rank, local)
 

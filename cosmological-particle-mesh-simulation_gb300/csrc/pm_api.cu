@@ -10,7 +10,8 @@ struct pm_ctx {
   int n = 0;
   Tables tab;
   SortBufs sort;
-  DBuf d_sim, d_prefix, d_err;
+  DBuf d_sim, d_prefix, d_err, d_maps;
+  const void* maps_for = nullptr;     // spectrum the device tensor maps describe
   DBuf row_start, spec, phi, rho;     // scratch grids
   DBuf hpos, hvel;                    // device copies for pm_step_host
   std::string err;
@@ -140,14 +141,14 @@ int spectral(pm_ctx* c, Call& k, bool table, cudaStream_t st, bool skip_r2c = fa
   const Sim* ds = c->d_sim.as<Sim>();
   const int n = c->n;
   const int gx = grid_for(k.prefix[PH_X][1], c->sms, 8), gl = grid_for(k.prefix[PH_LINE][1], c->sms, 8);
-  const void* sp = k.sim.spec;
+  const CUtensorMap* maps = c->maps_for ? c->d_maps.as<CUtensorMap>() : nullptr;
   int* err = c->d_err.as<int>();
-  if (!skip_r2c) PM_CK(spectral_dispatch(SPEC_X_R2C, n, ds, work(c, k, PH_X), gx, st, sp, 0, err), "x r2c");
-  PM_CK(spectral_dispatch(SPEC_Y_FWD, n, ds, work(c, k, PH_LINE), gl, st, sp, 0, err), "y fwd");
-  PM_CK(spectral_dispatch(table ? SPEC_Z_TABLE : SPEC_Z_GREEN, n, ds, work(c, k, PH_LINE), gl, st, sp, 0, err),
+  if (!skip_r2c) PM_CK(spectral_dispatch(SPEC_X_R2C, n, ds, work(c, k, PH_X), gx, st, maps, err), "x r2c");
+  PM_CK(spectral_dispatch(SPEC_Y_FWD, n, ds, work(c, k, PH_LINE), gl, st, maps, err), "y fwd");
+  PM_CK(spectral_dispatch(table ? SPEC_Z_TABLE : SPEC_Z_GREEN, n, ds, work(c, k, PH_LINE), gl, st, maps, err),
         "z green");
-  PM_CK(spectral_dispatch(SPEC_Y_INV, n, ds, work(c, k, PH_LINE), gl, st, sp, 0, err), "y inv");
-  PM_CK(spectral_dispatch(SPEC_X_C2R, n, ds, work(c, k, PH_X), gx, st, sp, 0, err), "x c2r");
+  PM_CK(spectral_dispatch(SPEC_Y_INV, n, ds, work(c, k, PH_LINE), gl, st, maps, err), "y inv");
+  PM_CK(spectral_dispatch(SPEC_X_C2R, n, ds, work(c, k, PH_X), gx, st, maps, err), "x c2r");
   return PM_OK;
 }
 
@@ -156,6 +157,16 @@ int prepare_spectral(pm_ctx* c, Call& k) {
   cudaError_t e = c->spec.ensure(sb);
   if (e) return cuda_fail(c, e, "alloc spectrum");
   k.sim.spec = c->spec.as<float2>();
+  if (c->maps_for != c->spec.p) {  // tensor maps of the spectrum for the TMA line passes
+    CUtensorMap m[2];
+    c->maps_for = nullptr;
+    if (spectral_encode_maps(c->n, c->spec.p, m)) {
+      e = c->d_maps.ensure(sizeof(m));
+      if (!e) e = cudaMemcpy(c->d_maps.p, m, sizeof(m), cudaMemcpyHostToDevice);
+      if (e) return cuda_fail(c, e, "tensor maps");
+      c->maps_for = c->spec.p;
+    }
+  }
   return PM_OK;
 }
 
@@ -221,6 +232,7 @@ void pm_ctx_destroy(pm_ctx* c) {
   c->d_sim.release();
   c->d_prefix.release();
   c->d_err.release();
+  c->d_maps.release();
   c->row_start.release();
   c->spec.release();
   c->phi.release();

@@ -66,7 +66,7 @@ struct pm_batch {
   long long pcap = 0;
   int cur = 0;
   SortBufs sort;
-  DBuf row_start, d_sims, d_prefix, d_err;
+  DBuf row_start, d_sims, d_prefix, d_err, d_maps;
   Plan plan;
   bool dirty = true, keys_valid = false;
   bool graphs = true;
@@ -178,9 +178,11 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   P = Plan();
   P.nsims = (int)b->sims.size();
   if (P.nsims == 0) return PM_OK;
-  int nmax = 0;
-  for (auto& s : b->sims) nmax = std::max(nmax, s->n);
-  P.xbits = ceil_log2(nmax);
+  // Resident keys are the global x-row number alone: the deposit needs particles grouped by
+  // row, not ordered inside a row (its integer sums do not depend on the order), and the
+  // stable sort keeps the previous step's order inside each row.  The key space is the
+  // batch's total number of rows (< 2^32).
+  P.xbits = 0;
   std::vector<Sim> hs(P.nsims);
   const int S = P.nsims;
   std::vector<int> pre;  // [phase][S+1]
@@ -191,12 +193,13 @@ int build_plan(pm_batch* b, cudaStream_t st) {
     r.part_off = off;
     r.row_base = rows;
     off += r.np;
+    if ((long long)rows + (long long)r.n * r.n >= (1ll << 32)) return bfail(b, PM_ERR_ADMIT, "too many x-rows");
     rows += (unsigned)((long long)r.n * r.n);
     if (std::find(P.sizes.begin(), P.sizes.end(), r.n) == P.sizes.end()) P.sizes.push_back(r.n);
   }
   P.ptot = off;
   P.rows = rows;
-  P.bits = ceil_log2((long long)rows) + P.xbits;
+  P.bits = ceil_log2((long long)rows) + P.xbits;  // keys are < rows
   if (P.bits > 32) return bfail(b, PM_ERR_ADMIT, "batch key space exceeds 32 bits");
   std::sort(P.sizes.begin(), P.sizes.end());
   const int nph = PH_FIXED + 3 * (int)P.sizes.size();
@@ -267,6 +270,14 @@ int build_plan(pm_batch* b, cudaStream_t st) {
       if (b->sims[i]->n == P.sizes[g]) { only = i; ++count; }
     P.single.push_back(count == 1 ? only : -1);
   }
+  {  // tensor maps of every spectrum (y pass, z pass) for the TMA line passes
+    std::vector<CUtensorMap> maps(2 * (size_t)S);
+    std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
+    for (int i = 0; i < S; ++i) spectral_encode_maps(b->sims[i]->n, b->sims[i]->spec.p, &maps[2 * i]);
+    PB_CK(b->d_maps.ensure(sizeof(CUtensorMap) * maps.size()), "alloc maps");
+    PB_CK(cudaMemcpyAsync(b->d_maps.p, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice, st),
+          "upload maps");
+  }
   PB_CK(b->d_sims.ensure(sizeof(Sim) * S), "alloc sims");
   PB_CK(b->d_prefix.ensure(sizeof(int) * pre.size()), "alloc prefix");
   PB_CK(b->row_start.ensure(sizeof(unsigned) * ((size_t)rows + 1)), "alloc rows");
@@ -309,11 +320,8 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
   int* err = b->d_err.as<int>();
   Parts in = state(b, cur), out = state(b, 1 - cur);
   bool alt = false;
-  // the deposit needs particles grouped by x-row only (its sums do not depend on the order
-  // inside a row): sort on the row bits of the key; the sort is stable, so the order inside
-  // a row is the previous step's order, itself sorted by cell
-  PB_CK(radix_sort(b->sort.keys.as<unsigned>(), b->sort.vals.as<unsigned>(), P.ptot, P.xbits, P.bits - P.xbits,
-                   true, b->sort.scratch(), &alt, st),
+  PB_CK(radix_sort(b->sort.keys.as<unsigned>(), b->sort.vals.as<unsigned>(), P.ptot, 0, P.bits, true,
+                   b->sort.scratch(), &alt, st),
         "sort");
   unsigned* perm = alt ? b->sort.vals_alt.as<unsigned>() : b->sort.vals.as<unsigned>();
   unsigned* skeys = alt ? b->sort.keys_alt.as<unsigned>() : b->sort.keys.as<unsigned>();
@@ -340,10 +348,8 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
       const bool xk = (k == SPEC_X_R2C || k == SPEC_X_C2R);
       const int ph = PH_FIXED + 3 * (int)g + (xk ? 0 : 1);
       const int tot = xk ? P.x_total[g] : P.line_total[g];
-      const int one = P.single[g];
-      const void* sp = one >= 0 ? b->sims[one]->spec.p : nullptr;
-      PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot), grid_for(tot, b->sms, 8), st, sp,
-                              one >= 0 ? one : 0, err),
+      PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot), grid_for(tot, b->sms, 8), st,
+                              b->d_maps.as<CUtensorMap>(), err),
             "spectral");
     }
     PB_CK(mark(1 + PP_X_R2C + o), "event");
@@ -360,7 +366,7 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
 // Kernel launches of one step for the current plan.
 int launches_per_step(pm_batch* b) {
   const Plan& P = b->plan;
-  const int passes = radix_sort_passes(P.bits - P.xbits);
+  const int passes = radix_sort_passes(P.bits);
   int n = 3 * passes + 1 + (P.fixed_total[PH_DEP] > 0 ? 1 : 0) + 5 * (int)P.sizes.size() + 1 + 1;
   return n;  // each fused size replaces its x R2C launch by the fused deposit
 }
@@ -502,6 +508,7 @@ void pm_batch_destroy(pm_batch* b) {
   b->d_sims.release();
   b->d_prefix.release();
   b->d_err.release();
+  b->d_maps.release();
   if (b->own) cudaStreamDestroy(b->own);
   delete b;
 }

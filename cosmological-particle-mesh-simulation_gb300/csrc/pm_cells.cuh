@@ -87,8 +87,10 @@ __device__ __forceinline__ Cell particle_cell(const Sim& S, const Parts& p, long
   return cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
 }
 
+// xbits == 0 (resident batches): the key is the x-row number alone
 __device__ __forceinline__ unsigned cell_key(const Sim& S, const Cell& c) {
-  return ((S.row_base + row_number(c.y, c.z, S.n)) << S.xbits) | (unsigned)c.x;
+  const unsigned row = S.row_base + row_number(c.y, c.z, S.n);
+  return S.xbits ? ((row << S.xbits) | (unsigned)c.x) : row;
 }
 
 // The 8 CIC weights in the order of integrate.py:44-51: [ttt, dtt, tdt, ttd, ddt, dtd, tdd, ddd]

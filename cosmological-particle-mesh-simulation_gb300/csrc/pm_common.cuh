@@ -9,6 +9,7 @@
 // Many simulations share one launch per phase: every kernel receives the device
 // array of `Sim` descriptors and a per-phase work prefix (CTA -> simulation).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -91,20 +92,22 @@ __device__ __forceinline__ void set_error(int* err, int code) {
 // spectral passes: one kernel per grid size n (supported n: spectral_supported)
 enum SpecKind : int { SPEC_X_R2C = 0, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Z_TABLE, SPEC_Y_INV, SPEC_X_C2R,
                       SPEC_PREPARE /* only set kernel attributes */ };
-// spec_single: the spectrum of the only simulation of size N in the launch, sims[sim_index]
-// (enables the TMA-streamed line passes for the sizes that have them); nullptr when
-// several simulations of size N share the launch.  The other kernels ignore both and
-// find their simulation through the work prefix.
+// maps: device array of tensor maps, two per simulation of `sims` (y pass, z pass; see
+// spectral_encode_maps) -- enables the TMA-streamed line passes; nullptr falls back to
+// plain loads.  Every kernel finds its simulation through the work prefix.
 template <int N>
 cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cudaStream_t st,
-                            const void* spec_single, int sim_index, int* err);
+                            const CUtensorMap* maps, int* err);
+// Encodes the y- and z-pass tensor maps of a half spectrum of size n (false if n has no
+// TMA line pass).
+bool spectral_encode_maps(int n, const void* spec, CUtensorMap out[2]);
 bool spectral_supported(int n);
 // work units (CTAs' worth of work) of one spectral pass for a grid of size n
 long long spectral_units(SpecKind kind, int n);
 // resident CTAs per SM of a spectral pass for size n (for persistent grid sizing)
 int spectral_ctas_per_sm(SpecKind kind, int n);
 cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int ctas, cudaStream_t st,
-                              const void* spec_single = nullptr, int sim_index = 0, int* err = nullptr);
+                              const CUtensorMap* maps = nullptr, int* err = nullptr);
 cudaError_t launch_fourier_grid(const Sim* sims, int ctas, cudaStream_t st);
 // fused deposit + x R2C (the density grid is not written); ctas <= 0 only prepares
 template <int N>

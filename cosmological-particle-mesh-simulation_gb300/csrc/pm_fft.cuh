@@ -1,7 +1,10 @@
 // Shared-memory Stockham FFT for batches of lines (radix 2, 3, 4, 8).
 //
-// A CTA holds NL lines of L complex elements in shared memory, element j of line l at
-// s[j * LS + l] (lines interleaved, so consecutive threads touch consecutive words).
+// A CTA holds NL lines of L complex elements in shared memory.  Two layouts:
+//   Interleaved<LS>: element j of line l at s[j * LS + l];
+//   Blocked<L, BW>:  lines in blocks of BW (a TMA box of BW columns), element j of line l at
+//                    s[(l / BW) * L * BW + j * BW + l % BW].
+// Either way consecutive threads (consecutive lines) touch consecutive words.
 // Each pass loads all of its butterflies into registers, synchronises, and writes the
 // self-sorted (Stockham) output back in place; the last pass leaves natural order.
 // Twiddles come from a table tw[m] = exp(-2 pi i m / (L * tws)) read with stride tws.
@@ -111,8 +114,20 @@ PM_PLAN(768, 3, 4, 8, 8)
 PM_PLAN(1024, 2, 8, 8, 8)
 #undef PM_PLAN
 
+template <int LS>
+struct Interleaved {
+  static __device__ __forceinline__ int at(int j, int line) { return j * LS + line; }
+};
+
+template <int L, int BW>
+struct Blocked {
+  static __device__ __forceinline__ int at(int j, int line) {
+    return (line / BW) * (L * BW) + j * BW + (line % BW);
+  }
+};
+
 // One Stockham pass of radix R on NL lines (in place through registers).
-template <int L, int R, int NS, int NL, int LS, int NT, bool INV>
+template <int L, int R, int NS, int NL, class LAY, int NT, bool INV>
 __device__ __forceinline__ void stockham_pass(float2* s, const float2* __restrict__ tw, int tws) {
   constexpr int NB = L / R;
   constexpr int NTASK = NL * NB;
@@ -124,7 +139,7 @@ __device__ __forceinline__ void stockham_pass(float2* s, const float2* __restric
     if ((NTASK % NT) == 0 || task < NTASK) {
       const int line = task % NL, j = task / NL;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[t][r] = s[(j + r * NB) * LS + line];
+      for (int r = 0; r < R; ++r) v[t][r] = s[LAY::at(j + r * NB, line)];
     }
   }
   __syncthreads();
@@ -145,18 +160,18 @@ __device__ __forceinline__ void stockham_pass(float2* s, const float2* __restric
       DFT<R, INV>::run(v[t]);
       const int base = (j - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; ++r) s[(base + r * NS) * LS + line] = v[t][r];
+      for (int r = 0; r < R; ++r) s[LAY::at(base + r * NS, line)] = v[t][r];
     }
   }
   __syncthreads();
 }
 
-template <int L, int P, int NS, int NL, int LS, int NT, bool INV>
+template <int L, int P, int NS, int NL, class LAY, int NT, bool INV>
 __device__ __forceinline__ void fft_passes(float2* s, const float2* __restrict__ tw, int tws) {
   if constexpr (P < Plan<L>::np) {
     constexpr int R = Plan<L>::r[P];
-    stockham_pass<L, R, NS, NL, LS, NT, INV>(s, tw, tws);
-    fft_passes<L, P + 1, NS * R, NL, LS, NT, INV>(s, tw, tws);
+    stockham_pass<L, R, NS, NL, LAY, NT, INV>(s, tw, tws);
+    fft_passes<L, P + 1, NS * R, NL, LAY, NT, INV>(s, tw, tws);
   }
 }
 
@@ -164,7 +179,13 @@ __device__ __forceinline__ void fft_passes(float2* s, const float2* __restrict__
 // Must be entered by all NT threads after a __syncthreads(); returns synchronised.
 template <int L, int NL, int LS, int NT, bool INV>
 __device__ __forceinline__ void fft_lines(float2* s, const float2* __restrict__ tw, int tws) {
-  fft_passes<L, 0, 1, NL, LS, NT, INV>(s, tw, tws);
+  fft_passes<L, 0, 1, NL, Interleaved<LS>, NT, INV>(s, tw, tws);
+}
+
+// Same on NL lines stored in blocks of BW lines (Blocked layout).
+template <int L, int NL, int BW, int NT, bool INV>
+__device__ __forceinline__ void fft_lines_blocked(float2* s, const float2* __restrict__ tw, int tws) {
+  fft_passes<L, 0, 1, NL, Blocked<L, BW>, NT, INV>(s, tw, tws);
 }
 
 }  // namespace pm

@@ -40,15 +40,18 @@ __host__ __device__ constexpr int cbundles_per_plane(int n) {
 }
 
 __host__ __device__ constexpr int cpitch(int n) { return (chalf(n) + 15) / 16 * 16; }
-// Line passes that stream through a TMA ring: one bundle per unit, whole 256-row boxes.
-__host__ __device__ constexpr bool tma_lines(int n) { return cline_bpc(n) == 1 && n % 256 == 0; }
+// Line passes that stream through a TMA ring: boxes of at most 256 rows tiling n.
+__host__ __device__ constexpr int line_box_rows(int n) { return n <= 256 ? n : (n % 256 == 0 ? 256 : n / 2); }
+__host__ __device__ constexpr bool tma_lines(int n) { return n >= 32 && line_box_rows(n) <= 256; }
 constexpr int TMA_NT = 512;
 constexpr int TMA_STAGES = 3;
-__host__ __device__ constexpr size_t tma_stage_bytes(int n) { return (size_t)n * cline_width(n) * sizeof(float2); }
+__host__ __device__ constexpr size_t tma_stage_bytes(int n) {
+  return (size_t)n * cline_width(n) * cline_bpc(n) * sizeof(float2);
+}
 __host__ __device__ constexpr size_t tma_smem_bytes(int n) { return TMA_STAGES * tma_stage_bytes(n) + 64; }
 
 // x passes fed by bulk copies into a double-buffered staging area (one simulation per launch)
-__host__ __device__ constexpr bool tma_rows(int n) { return n >= 256; }
+__host__ __device__ constexpr bool tma_rows(int n);
 __host__ __device__ constexpr int xrow_stage_floats(int n) { return n + 4; }  // (n/2 + 2) complex: bulk size % 16 == 0
 __host__ __device__ constexpr size_t xtma_fft_bytes(int n);
 __host__ __device__ constexpr size_t xtma_smem_bytes(int n);
@@ -64,6 +67,7 @@ __host__ __device__ constexpr size_t xtma_fft_bytes(int n) { return x_smem_bytes
 __host__ __device__ constexpr size_t xtma_smem_bytes(int n) {
   return 2 * (size_t)cx_rows(n) * xrow_stage_floats(n) * sizeof(float) + xtma_fft_bytes(n) + 64;
 }
+__host__ __device__ constexpr bool tma_rows(int n) { return n >= 32 && xtma_smem_bytes(n) <= 227 * 1024; }
 
 // ---------------------------------------------------------------------------------
 // x_r2c
@@ -315,27 +319,28 @@ __global__ void __launch_bounds__(SP_NT) k_z_green(const Sim* __restrict__ sims,
 }
 
 // ---------------------------------------------------------------------------------
-// TMA-streamed line pass (y forward / y inverse / z Green), one simulation per launch.
+// TMA-streamed line pass (y forward / y inverse / z Green) over one or many simulations.
 //
-// Persistent CTA with a 3-stage shared-memory ring.  One elected thread issues the TMA
-// load of bundle i+1 while all threads transform bundle i; finished bundles leave by TMA
-// bulk store, and a stage is refilled only once the store issued from it two iterations
-// earlier has finished reading it.  A bundle is BW consecutive kx of one plane, loaded as
-// n / 256 boxes of {2 BW floats, 256 rows}.
+// Persistent CTA with a 3-stage shared-memory ring.  A unit is BPC bundles of one
+// simulation; a bundle is BW consecutive kx of one plane, loaded as N / BOX TMA boxes of
+// {2 BW floats, BOX rows} with the simulation's tensor map (maps[2 s] for y, maps[2 s + 1]
+// for z, in device memory).  One elected thread issues the loads of unit i+1 while all
+// threads transform unit i; finished bundles leave by TMA bulk store, and a stage is
+// refilled only once the store issued from it two iterations earlier has finished
+// reading it.  Stages hold the bundles blocked (Blocked layout of pm_fft.cuh).
 // ---------------------------------------------------------------------------------
 template <int N, int MODE>  // MODE 0: y forward, 1: y inverse, 2: z Green, 3: z Green (caller table)
-__global__ void __launch_bounds__(TMA_NT, 1) k_line_tma(const __grid_constant__ CUtensorMap tm,
-                                                        const Sim* __restrict__ sims, int sim_index, int nunits,
-                                                        int* err) {
-  constexpr int BW = cline_width(N), NL = BW;
-  constexpr int BOX = 256, NBOX = N / BOX;
-  constexpr int NBP = cbundles_per_plane(N), W = chalf(N);
+__global__ void __launch_bounds__(TMA_NT, 1) k_line_tma(const CUtensorMap* __restrict__ maps,
+                                                        const Sim* __restrict__ sims, Work w, int* err) {
+  constexpr int BW = cline_width(N), BPC = cline_bpc(N), NL = BW * BPC;
+  constexpr int BOX = line_box_rows(N), NBOX = N / BOX;
+  constexpr int NBP = cbundles_per_plane(N), W = chalf(N), NB = N * NBP;
   constexpr unsigned STAGE = (unsigned)tma_stage_bytes(N);
+  constexpr unsigned BUNDLE = (unsigned)N * BW * sizeof(float2);
   constexpr bool ZAX = MODE >= 2;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   float2* stg0 = reinterpret_cast<float2*>(smem_raw);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + TMA_STAGES * STAGE);
-  const Sim& S = sims[sim_index];
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int i = 0; i < TMA_STAGES; ++i) mbar_init(&bar[i], 1);
@@ -343,28 +348,38 @@ __global__ void __launch_bounds__(TMA_NT, 1) k_line_tma(const __grid_constant__ 
   }
   __syncthreads();
   auto stage_ptr = [&](int st) { return stg0 + (size_t)st * (STAGE / sizeof(float2)); };
-  auto coords = [&](int unit, int b, int& c0, int& c1, int& c2) {
-    const int plane = unit / NBP, kx0 = (unit % NBP) * BW;
+  // unit -> (simulation, first bundle, bundles in the unit)
+  auto unit_info = [&](int unit, int& si, int& b0, int& cnt) {
+    si = locate_sim(w, unit);
+    b0 = (unit - __ldg(&w.prefix[si])) * BPC;
+    cnt = NB - b0 < BPC ? NB - b0 : BPC;
+  };
+  auto coords = [&](int b, int box, int& c0, int& c1, int& c2) {
+    const int plane = b / NBP, kx0 = (b % NBP) * BW;
     c0 = 2 * kx0;
-    c1 = ZAX ? plane : b * BOX;
-    c2 = ZAX ? b * BOX : plane;
+    c1 = ZAX ? plane : box * BOX;
+    c2 = ZAX ? box * BOX : plane;
   };
   auto issue_load = [&](int unit, int st) {
-    mbar_expect_tx(&bar[st], STAGE);
+    int si, b0, cnt;
+    unit_info(unit, si, b0, cnt);
+    const CUtensorMap* tm = &maps[2 * si + (ZAX ? 1 : 0)];
+    mbar_expect_tx(&bar[st], (unsigned)cnt * BUNDLE);
+    for (int i = 0; i < cnt; ++i)
 #pragma unroll
-    for (int b = 0; b < NBOX; ++b) {
-      int c0, c1, c2;
-      coords(unit, b, c0, c1, c2);
-      tma_load_3d(stage_ptr(st) + b * BOX * BW, &tm, c0, c1, c2, &bar[st]);
-    }
+      for (int box = 0; box < NBOX; ++box) {
+        int c0, c1, c2;
+        coords(b0 + i, box, c0, c1, c2);
+        tma_load_3d(stage_ptr(st) + (i * N + box * BOX) * BW, tm, c0, c1, c2, &bar[st]);
+      }
   };
   int unit = blockIdx.x;
-  if (threadIdx.x == 0 && unit < nunits) issue_load(unit, 0);
+  if (threadIdx.x == 0 && unit < w.total) issue_load(unit, 0);
   unsigned parity = 0;  // bit st: parity of the next phase of stage st
-  for (int it = 0; unit < nunits; unit += gridDim.x, ++it) {
+  for (int it = 0; unit < w.total; unit += gridDim.x, ++it) {
     const int st = it % TMA_STAGES;
     const int next = unit + gridDim.x;
-    if (threadIdx.x == 0 && next < nunits) {
+    if (threadIdx.x == 0 && next < w.total) {
       bulk_wait_read<TMA_STAGES - 2>();  // the store that last read stage (it+1)%3 is done
       issue_load(next, (it + 1) % TMA_STAGES);
     }
@@ -374,19 +389,23 @@ __global__ void __launch_bounds__(TMA_NT, 1) k_line_tma(const __grid_constant__ 
       if (threadIdx.x == 0) set_error(err, ERR_TIMEOUT);
       break;
     }
+    int si, b0, cnt;
+    unit_info(unit, si, b0, cnt);
+    const Sim& S = sims[si];
     float2* s = stage_ptr(st);
     if (MODE == 0) {
-      fft_lines<N, NL, NL, TMA_NT, false>(s, S.tw, 1);
+      fft_lines_blocked<N, NL, BW, TMA_NT, false>(s, S.tw, 1);
     } else if (MODE == 1) {
-      fft_lines<N, NL, NL, TMA_NT, true>(s, S.tw, 1);
+      fft_lines_blocked<N, NL, BW, TMA_NT, true>(s, S.tw, 1);
     } else {
-      fft_lines<N, NL, NL, TMA_NT, false>(s, S.tw, 1);
+      fft_lines_blocked<N, NL, BW, TMA_NT, false>(s, S.tw, 1);
       const float g0 = S.green;
-      const int ky = unit / NBP, kxb = (unit % NBP) * BW;
       for (int e = threadIdx.x; e < N * NL; e += TMA_NT) {
-        const int kz = e / NL, kx = kxb + e % NL;
+        const int i = e / (N * BW), kz = (e / BW) % N, c = e % BW;
+        const int b = b0 + i;
+        const int ky = b / NBP, kx = (b % NBP) * BW + c;
         float g = 0.f;
-        if (kx < W) {
+        if (i < cnt && kx < W) {
           if (MODE == 3) {
             g = g0 * __ldg(&S.fgrid[((long long)kz * N + ky) * N + kx]);
           } else if ((kx | ky | kz) != 0) {
@@ -397,21 +416,58 @@ __global__ void __launch_bounds__(TMA_NT, 1) k_line_tma(const __grid_constant__ 
         s[e] = make_float2(v.x * g, v.y * g);
       }
       __syncthreads();
-      fft_lines<N, NL, NL, TMA_NT, true>(s, S.tw, 1);
+      fft_lines_blocked<N, NL, BW, TMA_NT, true>(s, S.tw, 1);
     }
     fence_proxy_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
+      const CUtensorMap* tm = &maps[2 * si + (ZAX ? 1 : 0)];
+      for (int i = 0; i < cnt; ++i)
 #pragma unroll
-      for (int b = 0; b < NBOX; ++b) {
-        int c0, c1, c2;
-        coords(unit, b, c0, c1, c2);
-        tma_store_3d(&tm, c0, c1, c2, s + b * BOX * BW);
-      }
+        for (int box = 0; box < NBOX; ++box) {
+          int c0, c1, c2;
+          coords(b0 + i, box, c0, c1, c2);
+          tma_store_3d(tm, c0, c1, c2, s + (i * N + box * BOX) * BW);
+        }
       bulk_commit();
     }
   }
   if (threadIdx.x == 0) bulk_wait<0>();
+}
+
+// Tensor map of a half spectrum seen as float32 [z][y][2*pitch], box {2 BW, BOX, 1} for the
+// y pass and {2 BW, 1, BOX} for the z pass.
+inline bool encode_spectrum_map(CUtensorMap* tm, const void* spec, int n, bool zaxis) {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+      return false;
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  const cuuint64_t row = (cuuint64_t)2 * cpitch(n);
+  const cuuint32_t box_rows = (cuuint32_t)line_box_rows(n);
+  cuuint64_t dims[3] = {row, (cuuint64_t)n, (cuuint64_t)n};
+  cuuint64_t strides[2] = {row * 4, row * 4 * (cuuint64_t)n};
+  cuuint32_t box[3] = {(cuuint32_t)(2 * cline_width(n)), zaxis ? 1u : box_rows, zaxis ? box_rows : 1u};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(spec), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+inline int device_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
 }
 
 // ---------------------------------------------------------------------------------
@@ -423,8 +479,7 @@ __global__ void __launch_bounds__(TMA_NT, 1) k_line_tma(const __grid_constant__ 
 // once with unit i+2, and the transform and its coalesced global stores follow.
 // ---------------------------------------------------------------------------------
 template <int N, bool C2R>
-__global__ void __launch_bounds__(TMA_NT, 1) k_x_tma(const Sim* __restrict__ sims, int sim_index, int nunits,
-                                                     int* err) {
+__global__ void __launch_bounds__(TMA_NT, 1) k_x_tma(const Sim* __restrict__ sims, Work w, int* err) {
   constexpr int M = N / 2, NR = cx_rows(N), LS = NR + 1, RS = xrow_stage_floats(N);
   constexpr int NT = TMA_NT;
   // bytes copied per row: R2C reads n floats; C2R reads M + 2 complex (= RS floats)
@@ -434,8 +489,8 @@ __global__ void __launch_bounds__(TMA_NT, 1) k_x_tma(const Sim* __restrict__ sim
                      reinterpret_cast<float*>(smem_raw + (size_t)NR * RS * sizeof(float))};
   float2* F = reinterpret_cast<float2*>(smem_raw + 2 * (size_t)NR * RS * sizeof(float));
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + 2 * (size_t)NR * RS * sizeof(float) + xtma_fft_bytes(N));
-  const Sim& S = sims[sim_index];
   const long long nrows = (long long)N * N;
+  const int nunits = w.total;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
@@ -445,7 +500,9 @@ __global__ void __launch_bounds__(TMA_NT, 1) k_x_tma(const Sim* __restrict__ sim
   __syncthreads();
   // warp 0 issues the copies of one unit: lane r copies rows r, r + 32, ...
   auto issue = [&](int unit, int st) {
-    const long long row0 = (long long)unit * NR;
+    const int si = locate_sim(w, unit);
+    const Sim& S = sims[si];
+    const long long row0 = (long long)(unit - __ldg(&w.prefix[si])) * NR;
     const int rows = (int)(nrows - row0 < NR ? nrows - row0 : NR);
     if (lane == 0) mbar_expect_tx(&bar[st], (unsigned)rows * ROWB);
     __syncwarp();
@@ -462,7 +519,9 @@ __global__ void __launch_bounds__(TMA_NT, 1) k_x_tma(const Sim* __restrict__ sim
   unsigned parity = 0;
   for (int it = 0; unit < nunits; unit += gridDim.x, ++it) {
     const int st = it & 1;
-    const long long row0 = (long long)unit * NR;
+    const int si = locate_sim(w, unit);
+    const Sim& S = sims[si];
+    const long long row0 = (long long)(unit - __ldg(&w.prefix[si])) * NR;
     const bool ok = mbar_wait(&bar[st], (parity >> st) & 1u);
     parity ^= 1u << st;
     if (__syncthreads_or(!ok)) {
@@ -607,43 +666,6 @@ cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned*
   }
 }
 
-// Tensor map of a half spectrum seen as float32 [z][y][2*pitch], box {2 BW, 256, 1} for the
-// y pass and {2 BW, 1, 256} for the z pass.
-inline bool encode_spectrum_map(CUtensorMap* tm, const void* spec, int n, bool zaxis) {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-            cudaSuccess ||
-        q != cudaDriverEntryPointSuccess || !p)
-      return false;
-    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
-  const cuuint64_t row = (cuuint64_t)2 * cpitch(n);
-  cuuint64_t dims[3] = {row, (cuuint64_t)n, (cuuint64_t)n};
-  cuuint64_t strides[2] = {row * 4, row * 4 * (cuuint64_t)n};
-  cuuint32_t box[3] = {(cuuint32_t)(2 * cline_width(n)), zaxis ? 1u : 256u, zaxis ? 256u : 1u};
-  cuuint32_t estr[3] = {1, 1, 1};
-  return fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(spec), dims, strides, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-inline int device_sms() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
-  return sms;
-}
-
-// ---------------------------------------------------------------------------------
-// per-N launcher (explicitly instantiated once per N in pm_spectral_n.cu)
-// ---------------------------------------------------------------------------------
 template <typename K>
 static cudaError_t max_shared(K kern, size_t bytes) {
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -653,7 +675,7 @@ static cudaError_t max_shared(K kern, size_t bytes) {
 
 template <int N>
 cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cudaStream_t st,
-                            const void* spec_single, int sim_index, int* err) {
+                            const CUtensorMap* maps, int* err) {
   static bool init = false;
   const size_t xs = x_smem_bytes(N), ls = line_smem_bytes(N);
   if (!init) {
@@ -678,36 +700,28 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
     if (e) return e;
     init = true;
   }
+  if (kind == SPEC_PREPARE) return cudaSuccess;
+  const int grid = w.total < device_sms() ? w.total : device_sms();
   if constexpr (tma_rows(N)) {
-    if (spec_single && (kind == SPEC_X_R2C || kind == SPEC_X_C2R)) {
-      const int units = (int)(((long long)N * N + cx_rows(N) - 1) / cx_rows(N));
-      const int grid = units < device_sms() ? units : device_sms();
-      if (kind == SPEC_X_R2C)
-        k_x_tma<N, false><<<grid, TMA_NT, xtma_smem_bytes(N), st>>>(sims, sim_index, units, err);
-      else
-        k_x_tma<N, true><<<grid, TMA_NT, xtma_smem_bytes(N), st>>>(sims, sim_index, units, err);
+    if (kind == SPEC_X_R2C || kind == SPEC_X_C2R) {
+      if (kind == SPEC_X_R2C) k_x_tma<N, false><<<grid, TMA_NT, xtma_smem_bytes(N), st>>>(sims, w, err);
+      else k_x_tma<N, true><<<grid, TMA_NT, xtma_smem_bytes(N), st>>>(sims, w, err);
       return cudaGetLastError();
     }
   }
   if constexpr (tma_lines(N)) {
-    if (spec_single && kind != SPEC_PREPARE && kind != SPEC_X_R2C && kind != SPEC_X_C2R) {
-      const bool zax = (kind == SPEC_Z_GREEN || kind == SPEC_Z_TABLE);
-      CUtensorMap tm;
-      if (!encode_spectrum_map(&tm, spec_single, N, zax)) return cudaErrorInvalidValue;
-      const int units = N * cbundles_per_plane(N);
-      const int grid = units < device_sms() ? units : device_sms();
+    if (maps) {
       const size_t sm = tma_smem_bytes(N);
       switch (kind) {
-        case SPEC_Y_FWD: k_line_tma<N, 0><<<grid, TMA_NT, sm, st>>>(tm, sims, sim_index, units, err); break;
-        case SPEC_Y_INV: k_line_tma<N, 1><<<grid, TMA_NT, sm, st>>>(tm, sims, sim_index, units, err); break;
-        case SPEC_Z_GREEN: k_line_tma<N, 2><<<grid, TMA_NT, sm, st>>>(tm, sims, sim_index, units, err); break;
-        default: k_line_tma<N, 3><<<grid, TMA_NT, sm, st>>>(tm, sims, sim_index, units, err); break;
+        case SPEC_Y_FWD: k_line_tma<N, 0><<<grid, TMA_NT, sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Y_INV: k_line_tma<N, 1><<<grid, TMA_NT, sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Z_GREEN: k_line_tma<N, 2><<<grid, TMA_NT, sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Z_TABLE: k_line_tma<N, 3><<<grid, TMA_NT, sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        default: break;
       }
-      return cudaGetLastError();
     }
   }
   switch (kind) {
-    case SPEC_PREPARE: return cudaSuccess;
     case SPEC_X_R2C: k_x_r2c<N><<<ctas, SP_NT, xs, st>>>(sims, w); break;
     case SPEC_X_C2R: k_x_c2r<N><<<ctas, SP_NT, xs, st>>>(sims, w); break;
     case SPEC_Y_FWD: k_y_pass<N, false><<<ctas, SP_NT, ls, st>>>(sims, w); break;

@@ -6,7 +6,7 @@ namespace pm {
 
 #define PM_FOR_EACH_N(X) X(16) X(24) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768) X(1024)
 
-#define PM_EXTERN(NN) extern template cudaError_t spectral_launch<NN>(SpecKind, const Sim*, Work, int, cudaStream_t, const void*, int, int*);
+#define PM_EXTERN(NN) extern template cudaError_t spectral_launch<NN>(SpecKind, const Sim*, Work, int, cudaStream_t, const CUtensorMap*, int*);
 PM_FOR_EACH_N(PM_EXTERN)
 #undef PM_EXTERN
 #define PM_EXTERN(NN)                                                                                         \
@@ -23,6 +23,11 @@ cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const 
 #undef PM_CASE
     default: return cudaErrorInvalidValue;
   }
+}
+
+bool spectral_encode_maps(int n, const void* spec, CUtensorMap out[2]) {
+  if (!tma_lines(n) || !spectral_supported(n)) return false;
+  return encode_spectrum_map(&out[0], spec, n, false) && encode_spectrum_map(&out[1], spec, n, true);
 }
 
 bool deposit_r2c_supported(int n) { return (TZ * TY * n) % DEP_NT == 0; }
@@ -53,9 +58,9 @@ int spectral_ctas_per_sm(SpecKind kind, int n) {
 }
 
 cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int ctas, cudaStream_t st,
-                              const void* spec_single, int sim_index, int* err) {
+                              const CUtensorMap* maps, int* err) {
   switch (n) {
-#define PM_CASE(NN) case NN: return spectral_launch<NN>(kind, sims, w, ctas, st, spec_single, sim_index, err);
+#define PM_CASE(NN) case NN: return spectral_launch<NN>(kind, sims, w, ctas, st, maps, err);
     PM_FOR_EACH_N(PM_CASE)
 #undef PM_CASE
     default: return cudaErrorInvalidValue;

@@ -6,7 +6,7 @@
 #endif
 
 namespace pm {
-template cudaError_t spectral_launch<PM_N>(SpecKind, const Sim*, Work, int, cudaStream_t, const void*, int, int*);
+template cudaError_t spectral_launch<PM_N>(SpecKind, const Sim*, Work, int, cudaStream_t, const CUtensorMap*, int*);
 template cudaError_t deposit_r2c_launch<PM_N>(const Sim*, Work, Parts, const unsigned*, const unsigned*, int, int*,
                                               int, cudaStream_t);
 }

@@ -2,13 +2,15 @@
 
 Follows src/gaussian_random_field.py:9-123 and src/zeldovich.py:10-100 of the
 reference operation for operation (same random stream, same float32/float64 mix), with
-two decisions that make the result well defined:
+three decisions that make the result well defined:
 
 * entries that the reference computes with ``np.divide``/``np.power`` ``where=`` and no
   ``out=`` (k = 0; left uninitialised there) are 0;
 * the Zel'dovich jitter (uniform in [-2, 2) cells, zeldovich.py:89-91), drawn from the
   unseeded stdlib ``random`` in the reference, is drawn from
-  ``numpy.random.Generator(PCG64(seed))``: x-jitter, then y, then z.
+  ``numpy.random.Generator(PCG64(seed))``: x-jitter, then y, then z;
+* a polar Box-Muller pair whose float32 u^2 + v^2 rounds up to >= 1 (NaN or a negative
+  square root in the reference's float32 expression) is evaluated in float64, clamped at 0.
 
 This runs once per simulation and is not part of the per-step path.
 """
@@ -64,8 +66,19 @@ def gaussian_random_numbers(n_parts: int, seed: int):
     s = u ** 2 + v ** 2
     shape = (n_parts,) * 3
     u, v, s = u.reshape(shape), v.reshape(shape), s.reshape(shape)
-    f1 = u * (-2 * np.log(s) / s) ** 0.5
-    f2 = v * (-2 * np.log(s) / s) ** 0.5
+    with np.errstate(invalid="ignore", divide="ignore"):
+        t = -2 * np.log(s) / s
+    # float32 rounding can take u^2 + v^2 (< 1 in float64) to >= 1, making t <= 0 or NaN
+    # (the reference computes the same float32 expression); those rare entries are
+    # recomputed in float64 and clamped at 0
+    bad = ~(t > 0)
+    if bad.any():
+        s64 = u[bad].astype(np.float64) ** 2 + v[bad].astype(np.float64) ** 2
+        with np.errstate(invalid="ignore", divide="ignore"):
+            t64 = -2.0 * np.log(s64) / s64
+        t[bad] = np.where(np.isfinite(t64) & (t64 > 0), t64, 0.0).astype(np.float32)
+    f1 = u * t ** 0.5
+    f2 = v * t ** 0.5
     return f1, f2
 
 
