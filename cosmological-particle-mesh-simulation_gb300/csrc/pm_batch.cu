@@ -522,6 +522,11 @@ int pm_batch_set_graphs(pm_batch* b, int enable) {
   return PM_OK;
 }
 
+int pm_batch_admits(pm_batch* b, const pm_config* cfg) {
+  if (!b || !cfg) return 0;
+  return (!b->cap || used_bytes(b) + footprint(*cfg) <= b->cap) ? 1 : 0;
+}
+
 int pm_batch_add(pm_batch* b, const pm_config* cfg, const float* positions, const float* velocities,
                  int on_device, int* sim_id) {
   if (!b) return PM_ERR_ARG;

@@ -91,6 +91,7 @@ __device__ __forceinline__ void set_error(int* err, int code) {
 // ---------------------------------------------------------------------------------
 // spectral passes: one kernel per grid size n (supported n: spectral_supported)
 enum SpecKind : int { SPEC_X_R2C = 0, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Z_TABLE, SPEC_Y_INV, SPEC_X_C2R,
+                      SPEC_Z_FWD, SPEC_Z_INV, /* plain z transforms (initial conditions) */
                       SPEC_PREPARE /* only set kernel attributes */ };
 // maps: device array of tensor maps, two per simulation of `sims` (y pass, z pass; see
 // spectral_encode_maps) -- enables the TMA-streamed line passes; nullptr falls back to

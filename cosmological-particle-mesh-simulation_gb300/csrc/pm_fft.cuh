@@ -126,9 +126,16 @@ struct Blocked {
   }
 };
 
-// One Stockham pass of radix R on NL lines (in place through registers).
-template <int L, int R, int NS, int NL, class LAY, int NT, bool INV>
-__device__ __forceinline__ void stockham_pass(float2* s, const float2* __restrict__ tw, int tws) {
+// No-op epilogue of a pass.
+struct NoEpi {
+  __device__ __forceinline__ float2 operator()(float2 v, int /*j*/, int /*line*/) const { return v; }
+};
+
+// One Stockham pass of radix R on NL lines (in place through registers).  `epi` maps each
+// output value (element j of `line`) before it is stored.
+template <int L, int R, int NS, int NL, class LAY, int NT, bool INV, class EPI = NoEpi>
+__device__ __forceinline__ void stockham_pass(float2* s, const float2* __restrict__ tw, int tws,
+                                              const EPI& epi = EPI()) {
   constexpr int NB = L / R;
   constexpr int NTASK = NL * NB;
   constexpr int TPT = (NTASK + NT - 1) / NT;
@@ -160,18 +167,23 @@ __device__ __forceinline__ void stockham_pass(float2* s, const float2* __restric
       DFT<R, INV>::run(v[t]);
       const int base = (j - k) * R + k;
 #pragma unroll
-      for (int r = 0; r < R; ++r) s[LAY::at(base + r * NS, line)] = v[t][r];
+      for (int r = 0; r < R; ++r) s[LAY::at(base + r * NS, line)] = epi(v[t][r], base + r * NS, line);
     }
   }
   __syncthreads();
 }
 
-template <int L, int P, int NS, int NL, class LAY, int NT, bool INV>
-__device__ __forceinline__ void fft_passes(float2* s, const float2* __restrict__ tw, int tws) {
+template <int L, int P, int NS, int NL, class LAY, int NT, bool INV, class EPI = NoEpi>
+__device__ __forceinline__ void fft_passes(float2* s, const float2* __restrict__ tw, int tws,
+                                           const EPI& epi = EPI()) {
   if constexpr (P < Plan<L>::np) {
     constexpr int R = Plan<L>::r[P];
-    stockham_pass<L, R, NS, NL, LAY, NT, INV>(s, tw, tws);
-    fft_passes<L, P + 1, NS * R, NL, LAY, NT, INV>(s, tw, tws);
+    if constexpr (P + 1 == Plan<L>::np) {
+      stockham_pass<L, R, NS, NL, LAY, NT, INV, EPI>(s, tw, tws, epi);  // last pass: natural order
+    } else {
+      stockham_pass<L, R, NS, NL, LAY, NT, INV>(s, tw, tws);
+      fft_passes<L, P + 1, NS * R, NL, LAY, NT, INV, EPI>(s, tw, tws, epi);
+    }
   }
 }
 
@@ -182,10 +194,12 @@ __device__ __forceinline__ void fft_lines(float2* s, const float2* __restrict__ 
   fft_passes<L, 0, 1, NL, Interleaved<LS>, NT, INV>(s, tw, tws);
 }
 
-// Same on NL lines stored in blocks of BW lines (Blocked layout).
-template <int L, int NL, int BW, int NT, bool INV>
-__device__ __forceinline__ void fft_lines_blocked(float2* s, const float2* __restrict__ tw, int tws) {
-  fft_passes<L, 0, 1, NL, Blocked<L, BW>, NT, INV>(s, tw, tws);
+// Same on NL lines stored in blocks of BW lines (Blocked layout); `epi` maps every output
+// value (element j of line) as the last pass stores it.
+template <int L, int NL, int BW, int NT, bool INV, class EPI = NoEpi>
+__device__ __forceinline__ void fft_lines_blocked(float2* s, const float2* __restrict__ tw, int tws,
+                                                  const EPI& epi = EPI()) {
+  fft_passes<L, 0, 1, NL, Blocked<L, BW>, NT, INV, EPI>(s, tw, tws, epi);
 }
 
 }  // namespace pm

@@ -43,7 +43,10 @@ __host__ __device__ constexpr int cpitch(int n) { return (chalf(n) + 15) / 16 * 
 // Line passes that stream through a TMA ring: boxes of at most 256 rows tiling n.
 __host__ __device__ constexpr int line_box_rows(int n) { return n <= 256 ? n : (n % 256 == 0 ? 256 : n / 2); }
 __host__ __device__ constexpr bool tma_lines(int n) { return n >= 32 && line_box_rows(n) <= 256; }
-constexpr int TMA_NT = 512;
+// Threads of a line-pass CTA: 1024 (64 registers each) where the transform fits in them;
+// the small odd sizes keep 512 (128 registers) to stay clear of spills.
+__host__ __device__ constexpr int line_nt(int n) { return n % 3 == 0 && n < 192 ? 512 : 1024; }
+constexpr int XTMA_NT = 1024;  // x passes
 constexpr int TMA_STAGES = 3;
 __host__ __device__ constexpr size_t tma_stage_bytes(int n) {
   return (size_t)n * cline_width(n) * cline_bpc(n) * sizeof(float2);
@@ -254,22 +257,23 @@ __device__ __forceinline__ void store_bundles(const Sim& S, int unit, const floa
   }
 }
 
-template <int N, bool INV>
-__device__ __forceinline__ void y_body(const Sim& S, int unit, float2* s) {
+// Plain transform of the bundles of one unit along y (ZAXIS false) or z.
+template <int N, bool ZAXIS, bool INV>
+__device__ __forceinline__ void line_body(const Sim& S, int unit, float2* s) {
   constexpr int NL = cline_width(N) * cline_bpc(N);
-  load_bundles<N, false>(S, unit, s);
+  load_bundles<N, ZAXIS>(S, unit, s);
   __syncthreads();
   fft_lines<N, NL, NL, SP_NT, INV>(s, S.tw, 1);
-  store_bundles<N, false>(S, unit, s);
+  store_bundles<N, ZAXIS>(S, unit, s);
 }
 
-template <int N, bool INV>
-__global__ void __launch_bounds__(SP_NT) k_y_pass(const Sim* __restrict__ sims, Work w) {
+template <int N, bool ZAXIS, bool INV>
+__global__ void __launch_bounds__(SP_NT) k_line_pass(const Sim* __restrict__ sims, Work w) {
   extern __shared__ float4 smem_f4[];
   float2* s = reinterpret_cast<float2*>(smem_f4);
   for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
     const int si = locate_sim(w, unit);
-    y_body<N, INV>(sims[si], unit - __ldg(&w.prefix[si]), s);
+    line_body<N, ZAXIS, INV>(sims[si], unit - __ldg(&w.prefix[si]), s);
     __syncthreads();
   }
 }
@@ -329,8 +333,31 @@ __global__ void __launch_bounds__(SP_NT) k_z_green(const Sim* __restrict__ sims,
 // refilled only once the store issued from it two iterations earlier has finished
 // reading it.  Stages hold the bundles blocked (Blocked layout of pm_fft.cuh).
 // ---------------------------------------------------------------------------------
-template <int N, int MODE>  // MODE 0: y forward, 1: y inverse, 2: z Green, 3: z Green (caller table)
-__global__ void __launch_bounds__(TMA_NT, 1) k_line_tma(const CUtensorMap* __restrict__ maps,
+// Green function of potential.py:15 / fourier_utils.py:15-16 (k = 0 -> 0; the 1/n^3 of the
+// unnormalised inverse transforms is folded into g0) for element kz of line `line` of a unit
+// of the z pass whose first bundle is b0.
+template <int N, bool TABLE>
+struct GreenEpi {
+  float g0;
+  const float* s2;
+  const float* fgrid;
+  int b0, cnt;
+  __device__ __forceinline__ float2 operator()(float2 v, int kz, int line) const {
+    constexpr int BW = cline_width(N), NBP = cbundles_per_plane(N), W = chalf(N);
+    const int i = line / BW, b = b0 + i;
+    const int ky = b / NBP, kx = (b % NBP) * BW + line % BW;
+    float g = 0.f;
+    if (i < cnt && kx < W) {
+      if (TABLE) g = g0 * __ldg(&fgrid[((long long)kz * N + ky) * N + kx]);
+      else if ((kx | ky | kz) != 0) g = __fdividef(g0, __ldg(&s2[kx]) + __ldg(&s2[ky]) + __ldg(&s2[kz]));
+    }
+    return make_float2(v.x * g, v.y * g);
+  }
+};
+
+// MODE 0: y forward, 1: y inverse, 2: z Green, 3: z Green (caller table), 4: z forward, 5: z inverse
+template <int N, int MODE>
+__global__ void __launch_bounds__(line_nt(N), 1) k_line_tma(const CUtensorMap* __restrict__ maps,
                                                         const Sim* __restrict__ sims, Work w, int* err) {
   constexpr int BW = cline_width(N), BPC = cline_bpc(N), NL = BW * BPC;
   constexpr int BOX = line_box_rows(N), NBOX = N / BOX;
@@ -393,30 +420,15 @@ __global__ void __launch_bounds__(TMA_NT, 1) k_line_tma(const CUtensorMap* __res
     unit_info(unit, si, b0, cnt);
     const Sim& S = sims[si];
     float2* s = stage_ptr(st);
-    if (MODE == 0) {
-      fft_lines_blocked<N, NL, BW, TMA_NT, false>(s, S.tw, 1);
-    } else if (MODE == 1) {
-      fft_lines_blocked<N, NL, BW, TMA_NT, true>(s, S.tw, 1);
+    if (MODE == 0 || MODE == 4) {
+      fft_lines_blocked<N, NL, BW, line_nt(N), false>(s, S.tw, 1);
+    } else if (MODE == 1 || MODE == 5) {
+      fft_lines_blocked<N, NL, BW, line_nt(N), true>(s, S.tw, 1);
     } else {
-      fft_lines_blocked<N, NL, BW, TMA_NT, false>(s, S.tw, 1);
-      const float g0 = S.green;
-      for (int e = threadIdx.x; e < N * NL; e += TMA_NT) {
-        const int i = e / (N * BW), kz = (e / BW) % N, c = e % BW;
-        const int b = b0 + i;
-        const int ky = b / NBP, kx = (b % NBP) * BW + c;
-        float g = 0.f;
-        if (i < cnt && kx < W) {
-          if (MODE == 3) {
-            g = g0 * __ldg(&S.fgrid[((long long)kz * N + ky) * N + kx]);
-          } else if ((kx | ky | kz) != 0) {
-            g = __fdividef(g0, __ldg(&S.s2[kx]) + __ldg(&S.s2[ky]) + __ldg(&S.s2[kz]));
-          }
-        }
-        const float2 v = s[e];
-        s[e] = make_float2(v.x * g, v.y * g);
-      }
-      __syncthreads();
-      fft_lines_blocked<N, NL, BW, TMA_NT, true>(s, S.tw, 1);
+      // forward z transform; the Green function is applied as the last pass stores
+      const GreenEpi<N, MODE == 3> epi{S.green, S.s2, S.fgrid, b0, cnt};
+      fft_lines_blocked<N, NL, BW, line_nt(N), false>(s, S.tw, 1, epi);
+      fft_lines_blocked<N, NL, BW, line_nt(N), true>(s, S.tw, 1);
     }
     fence_proxy_async_smem();
     __syncthreads();
@@ -479,9 +491,9 @@ inline int device_sms() {
 // once with unit i+2, and the transform and its coalesced global stores follow.
 // ---------------------------------------------------------------------------------
 template <int N, bool C2R>
-__global__ void __launch_bounds__(TMA_NT, 1) k_x_tma(const Sim* __restrict__ sims, Work w, int* err) {
+__global__ void __launch_bounds__(XTMA_NT, 1) k_x_tma(const Sim* __restrict__ sims, Work w, int* err) {
   constexpr int M = N / 2, NR = cx_rows(N), LS = NR + 1, RS = xrow_stage_floats(N);
-  constexpr int NT = TMA_NT;
+  constexpr int NT = XTMA_NT;
   // bytes copied per row: R2C reads n floats; C2R reads M + 2 complex (= RS floats)
   constexpr unsigned ROWB = C2R ? RS * 4u : N * 4u;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -689,12 +701,16 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
       if (!e) e = max_shared(k_line_tma<N, 1>, tma_smem_bytes(N));
       if (!e) e = max_shared(k_line_tma<N, 2>, tma_smem_bytes(N));
       if (!e) e = max_shared(k_line_tma<N, 3>, tma_smem_bytes(N));
+      if (!e) e = max_shared(k_line_tma<N, 4>, tma_smem_bytes(N));
+      if (!e) e = max_shared(k_line_tma<N, 5>, tma_smem_bytes(N));
       if (e) return e;
     }
     cudaError_t e = max_shared(k_x_r2c<N>, xs);
     if (!e) e = max_shared(k_x_c2r<N>, xs);
-    if (!e) e = max_shared(k_y_pass<N, false>, ls);
-    if (!e) e = max_shared(k_y_pass<N, true>, ls);
+    if (!e) e = max_shared(k_line_pass<N, false, false>, ls);
+    if (!e) e = max_shared(k_line_pass<N, false, true>, ls);
+    if (!e) e = max_shared(k_line_pass<N, true, false>, ls);
+    if (!e) e = max_shared(k_line_pass<N, true, true>, ls);
     if (!e) e = max_shared(k_z_green<N, false>, ls);
     if (!e) e = max_shared(k_z_green<N, true>, ls);
     if (e) return e;
@@ -704,8 +720,8 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
   const int grid = w.total < device_sms() ? w.total : device_sms();
   if constexpr (tma_rows(N)) {
     if (kind == SPEC_X_R2C || kind == SPEC_X_C2R) {
-      if (kind == SPEC_X_R2C) k_x_tma<N, false><<<grid, TMA_NT, xtma_smem_bytes(N), st>>>(sims, w, err);
-      else k_x_tma<N, true><<<grid, TMA_NT, xtma_smem_bytes(N), st>>>(sims, w, err);
+      if (kind == SPEC_X_R2C) k_x_tma<N, false><<<grid, XTMA_NT, xtma_smem_bytes(N), st>>>(sims, w, err);
+      else k_x_tma<N, true><<<grid, XTMA_NT, xtma_smem_bytes(N), st>>>(sims, w, err);
       return cudaGetLastError();
     }
   }
@@ -713,10 +729,12 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
     if (maps) {
       const size_t sm = tma_smem_bytes(N);
       switch (kind) {
-        case SPEC_Y_FWD: k_line_tma<N, 0><<<grid, TMA_NT, sm, st>>>(maps, sims, w, err); return cudaGetLastError();
-        case SPEC_Y_INV: k_line_tma<N, 1><<<grid, TMA_NT, sm, st>>>(maps, sims, w, err); return cudaGetLastError();
-        case SPEC_Z_GREEN: k_line_tma<N, 2><<<grid, TMA_NT, sm, st>>>(maps, sims, w, err); return cudaGetLastError();
-        case SPEC_Z_TABLE: k_line_tma<N, 3><<<grid, TMA_NT, sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Y_FWD: k_line_tma<N, 0><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Y_INV: k_line_tma<N, 1><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Z_GREEN: k_line_tma<N, 2><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Z_TABLE: k_line_tma<N, 3><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Z_FWD: k_line_tma<N, 4><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Z_INV: k_line_tma<N, 5><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
         default: break;
       }
     }
@@ -724,8 +742,10 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
   switch (kind) {
     case SPEC_X_R2C: k_x_r2c<N><<<ctas, SP_NT, xs, st>>>(sims, w); break;
     case SPEC_X_C2R: k_x_c2r<N><<<ctas, SP_NT, xs, st>>>(sims, w); break;
-    case SPEC_Y_FWD: k_y_pass<N, false><<<ctas, SP_NT, ls, st>>>(sims, w); break;
-    case SPEC_Y_INV: k_y_pass<N, true><<<ctas, SP_NT, ls, st>>>(sims, w); break;
+    case SPEC_Y_FWD: k_line_pass<N, false, false><<<ctas, SP_NT, ls, st>>>(sims, w); break;
+    case SPEC_Y_INV: k_line_pass<N, false, true><<<ctas, SP_NT, ls, st>>>(sims, w); break;
+    case SPEC_Z_FWD: k_line_pass<N, true, false><<<ctas, SP_NT, ls, st>>>(sims, w); break;
+    case SPEC_Z_INV: k_line_pass<N, true, true><<<ctas, SP_NT, ls, st>>>(sims, w); break;
     case SPEC_Z_GREEN: k_z_green<N, false><<<ctas, SP_NT, ls, st>>>(sims, w); break;
     case SPEC_Z_TABLE: k_z_green<N, true><<<ctas, SP_NT, ls, st>>>(sims, w); break;
     default: return cudaErrorInvalidValue;

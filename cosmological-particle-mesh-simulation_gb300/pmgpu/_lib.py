@@ -26,6 +26,11 @@ class PMConfigC(ctypes.Structure):
                 ("flags", c_int)]
 
 
+class PMICParamsC(ctypes.Structure):
+    _fields_ = [("power", c_double), ("lcdm_transfer", c_int), ("jitter_state", ctypes.c_ulonglong * 2),
+                ("jitter_inc", ctypes.c_ulonglong * 2)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "pm_ctx_create": (c_int, [ctypes.POINTER(PMConfigC), c_int, ctypes.POINTER(c_void_p)]),
@@ -46,11 +51,17 @@ SIGNATURES = {
     "pm_cosmo_f": (c_double, [c_double, c_double, c_double, c_double]),
     "pm_sort_keys": (c_int, [c_void_p, c_void_p, c_ll, c_void_p, c_void_p, c_void_p, c_void_p]),
     "pm_density_noalloc": (c_int, [c_void_p, c_ll, c_int, c_double, c_void_p, c_void_p]),
+    "pm_ics_create": (c_int, [c_int, c_int, ctypes.POINTER(c_void_p)]),
+    "pm_ics_destroy": (None, [c_void_p]),
+    "pm_ics_last_error": (c_char_p, [c_void_p]),
+    "pm_ics_generate": (c_int, [c_void_p, ctypes.POINTER(PMConfigC), ctypes.POINTER(PMICParamsC), c_void_p,
+                                c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "pm_batch_create": (c_int, [c_int, c_size_t, ctypes.POINTER(c_void_p)]),
     "pm_batch_destroy": (None, [c_void_p]),
     "pm_batch_last_error": (c_char_p, [c_void_p]),
     "pm_sim_footprint": (c_size_t, [ctypes.POINTER(PMConfigC)]),
     "pm_batch_add": (c_int, [c_void_p, ctypes.POINTER(PMConfigC), c_void_p, c_void_p, c_int, P_int]),
+    "pm_batch_admits": (c_int, [c_void_p, ctypes.POINTER(PMConfigC)]),
     "pm_batch_step": (c_int, [c_void_p, c_int, c_void_p]),
     "pm_batch_get": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, P_double, P_int, c_void_p]),
     "pm_batch_active": (c_int, [c_void_p, c_int]),

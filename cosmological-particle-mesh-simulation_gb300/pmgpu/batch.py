@@ -47,6 +47,10 @@ class Batch:
     def footprint(cfg: Config) -> int:
         return int(_lib.load().pm_sim_footprint(ctypes.byref(cfg.c_struct())))
 
+    def admits(self, cfg: Config) -> bool:
+        """Whether add(cfg, ...) would pass the memory cap now."""
+        return bool(self._lib.pm_batch_admits(self._h, ctypes.byref(cfg.c_struct())))
+
     def add(self, cfg: Config, positions, velocities) -> int:
         on_dev = isinstance(positions, torch.Tensor) and positions.is_cuda
         if on_dev:

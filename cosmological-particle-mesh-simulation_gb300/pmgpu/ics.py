@@ -47,8 +47,9 @@ def cosmo_Dt(a, om, ol, ok):
     return 5 / 2 / om / (om ** (4 / 7) - ol + (1 + om / 2) * (1 + ol / 70)) * a
 
 
-def gaussian_random_numbers(n_parts: int, seed: int):
-    """gaussian_random_field.py:31-63: rejection-sampled polar Box-Muller, float32."""
+def uniform_pairs(n_parts: int, seed: int):
+    """gaussian_random_field.py:35-50: the accepted (u, v) of the rejection loop, float32,
+    flat (N_PARTS^3,) each, from numpy's RandomState(seed)."""
     rs = np.random.RandomState(seed)
     total = n_parts ** 3
     u = np.zeros(total, dtype=np.float32)
@@ -63,6 +64,20 @@ def gaussian_random_numbers(n_parts: int, seed: int):
         u[acc:acc + len(u1)] = u1
         v[acc:acc + len(v1)] = v1
         acc += len(u1)
+    return u, v
+
+
+def jitter_state(seed: int):
+    """The 128-bit state and increment of numpy's PCG64(seed), the generator of the
+    Zel'dovich jitter, as (high, low) 64-bit word pairs."""
+    st = np.random.PCG64(seed).state["state"]
+    m = (1 << 64) - 1
+    return ((st["state"] >> 64) & m, st["state"] & m), ((st["inc"] >> 64) & m, st["inc"] & m)
+
+
+def gaussian_random_numbers(n_parts: int, seed: int):
+    """gaussian_random_field.py:31-63: rejection-sampled polar Box-Muller, float32."""
+    u, v = uniform_pairs(n_parts, seed)
     s = u ** 2 + v ** 2
     shape = (n_parts,) * 3
     u, v, s = u.reshape(shape), v.reshape(shape), s.reshape(shape)

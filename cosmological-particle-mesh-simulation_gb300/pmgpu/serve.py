@@ -1,10 +1,12 @@
 """Serving loop: simulation requests admitted by HBM footprint, stepped together.
 
-A request is (seed, N_PARTS, box, steps) on a 2 N_PARTS grid.  Its initial conditions are
-made on the host by a pool of worker processes as soon as it arrives; once they are ready
-and its footprint fits under the memory cap, it joins the resident batch (continuous
-batching: requests that arrive while others run are admitted as slots and memory free
-up).  The batch advances all resident simulations together, a few steps per tick; a
+A request is (seed, N_PARTS, box, steps) on a 2 N_PARTS grid.  As soon as it arrives a
+pool of worker processes draws its random stream on the host: the accepted uniform pairs
+of the reference's rejection loop (device_ics=True, the default; the Gaussian field and
+Zel'dovich step then run on the GPU at admission, milliseconds) or the whole initial
+conditions (device_ics=False).  Once they are ready and its footprint fits under the
+memory cap, it joins the resident batch (continuous batching: requests that arrive while
+others run are admitted as slots and memory free up).  The batch advances all resident simulations together, a few steps per tick; a
 finished simulation leaves the batch at once and its memory admits the next request.
 Latency = completion time - arrival time (initial conditions, queueing and stepping).
 """
@@ -55,9 +57,19 @@ def poisson_stream(rate: float, duration: float, seed: int = 0, sizes=(64, 96, 1
         rid += 1
 
 
-def _make_ics(req: Request):
+def _draw(req: Request, pairs_only: bool):
+    """Pool worker: the uniform pairs for device initial conditions, else the host ones."""
+    if pairs_only:
+        from .ics import uniform_pairs
+        return req.rid, uniform_pairs(req.n_parts, req.seed)
     from .ics import initial_conditions
     return req.rid, initial_conditions(req.config())
+
+
+def uses_device_ics(n_parts: int, device_ics: bool) -> bool:
+    """Device initial conditions need an FFT size the engine supports; other sizes use the host."""
+    from . import _lib
+    return device_ics and bool(_lib.load().pm_supported_n(n_parts))
 
 
 @dataclasses.dataclass
@@ -77,9 +89,14 @@ class Server:
     """Runs a request stream against one GPU in real time."""
 
     def __init__(self, mem_cap_bytes: int, ic_workers: int = 8, steps_per_tick: int = 4, device: int = 0,
-                 keep_results: bool = False):
+                 keep_results: bool = False, device_ics: bool = True):
+        import torch
         from .batch import Batch
         self.batch = Batch(device=device, mem_cap_bytes=mem_cap_bytes)
+        self.device = device
+        self.device_ics = device_ics
+        self._ics = {}  # N_PARTS -> DeviceICs
+        self._ic_stream = torch.cuda.Stream(device=device) if device_ics else None
         self.cap = mem_cap_bytes
         self.steps_per_tick = steps_per_tick
         self.pool = cf.ProcessPoolExecutor(max_workers=ic_workers, mp_context=mp.get_context("spawn"))
@@ -88,7 +105,20 @@ class Server:
 
     def close(self):
         self.pool.shutdown(wait=False, cancel_futures=True)
+        for g in self._ics.values():
+            g.close()
+        self._ics.clear()
         self.batch.close()
+
+    def _initial_state(self, r: Request, drawn):
+        """Positions/velocities to admit: host arrays, or generated on the GPU from the pairs."""
+        if not uses_device_ics(r.n_parts, self.device_ics):
+            return drawn
+        from .device_ics import DeviceICs
+        g = self._ics.get(r.n_parts)
+        if g is None:
+            g = self._ics[r.n_parts] = DeviceICs(r.n_parts, self.device)
+        return g.generate(r.config(), uv=drawn, stream=self._ic_stream)
 
     def run(self, stream: list[Request], time_limit: float | None = None) -> list[Result]:
         from .batch import Batch
@@ -107,7 +137,7 @@ class Server:
                 break
             while nxt < len(pending) and pending[nxt].arrival <= t:
                 r = pending[nxt]
-                futures[self.pool.submit(_make_ics, r)] = r
+                futures[self.pool.submit(_draw, r, uses_device_ics(r.n_parts, self.device_ics))] = r
                 queued.append(r)
                 nxt += 1
             for fu in [f for f in futures if f.done()]:
@@ -118,8 +148,13 @@ class Server:
             while queued and queued[0].rid in ready:
                 r = queued[0]
                 fp = Batch.footprint(r.config())
+                if self.cap and fp > self.cap:
+                    raise RuntimeError(f"request {r.rid} alone exceeds the memory cap")
+                if not self.batch.admits(r.config()):
+                    break  # wait for memory to free up
+                state = self._initial_state(r, ready[r.rid])
                 try:
-                    sid = self.batch.add(r.config(), *ready[r.rid])
+                    sid = self.batch.add(r.config(), *state)
                 except PMError as e:  # refused: over the memory cap -> wait for memory to free up
                     if e.code != PM_ERR_ADMIT:
                         raise

@@ -122,6 +122,30 @@ int pm_sort_keys(pm_ctx* ctx, const float* positions, long long np, unsigned* ke
 int pm_density_noalloc(const float* positions, long long np, int n_cells, double mass, float* rho,
                        void* stream);
 
+/* ---- initial conditions on the device -------------------------------------------- */
+/* Parameters of src/gaussian_random_field.py and of the Zel'dovich jitter. */
+typedef struct pm_ic_params {
+  double power;                       /* POWER (configure_me.py:31) */
+  int lcdm_transfer;                  /* LCDM_TRANSFER_FUNCTION (configure_me.py:32) */
+  unsigned long long jitter_state[2]; /* numpy PCG64(RANDOM_SEED) 128-bit state: high, low word */
+  unsigned long long jitter_inc[2];   /* its increment: high, low word */
+} pm_ic_params;
+
+typedef struct pm_ics pm_ics;
+
+/* Scratch and tables for N_PARTS^3 initial conditions (N_PARTS: a pm_supported_n size). */
+int pm_ics_create(int n_parts, int device, pm_ics** out);
+void pm_ics_destroy(pm_ics* g);
+const char* pm_ics_last_error(const pm_ics* g);
+/* src/gaussian_random_field.py:9-123 then src/zeldovich.py:10-100 on the device.
+   u, v: the N_PARTS^3 accepted uniform pairs of the reference's rejection loop
+   (gaussian_random_field.py:35-50), float32.  Writes positions and velocities (3, N_PARTS^3)
+   and, when grf != NULL, the random field (N_PARTS^3).  The jitter (uniform in [-2, 2),
+   zeldovich.py:89-91) is numpy's PCG64 stream from jitter_state / jitter_inc: x draws, then
+   y, then z.  Device pointers; returns after the work on `stream` has completed. */
+int pm_ics_generate(pm_ics* g, const pm_config* cfg, const pm_ic_params* ic, const float* u,
+                    const float* v, float* positions, float* velocities, float* grf, void* stream);
+
 /* ---- resident engine: batches of simulations ------------------------------------ */
 typedef struct pm_batch pm_batch;
 
@@ -135,6 +159,8 @@ size_t pm_sim_footprint(const pm_config* cfg);
    on_device selects device or host input arrays.  PM_ERR_ADMIT if over the cap. */
 int pm_batch_add(pm_batch* b, const pm_config* cfg, const float* positions,
                  const float* velocities, int on_device, int* sim_id);
+/* 1 if pm_batch_add of this configuration would pass the memory cap now, else 0. */
+int pm_batch_admits(pm_batch* b, const pm_config* cfg);
 /* Advances every active simulation by up to nsteps steps (a simulation stops after the
    src/pmesh.py:56 loop count).  Work is enqueued on `stream` (CUDA graphs). */
 int pm_batch_step(pm_batch* b, int nsteps, void* stream);

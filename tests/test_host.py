@@ -85,3 +85,93 @@ def test_initial_conditions_match_reference(name):
     pos, vel = ics.zeldovich(f["grf"], cfg)
     assert periodic_maxdiff(pos, f["pos0"], cfg.n_cells) < 8 * np.spacing(np.float32(cfg.n_cells))
     assert np.abs(vel - f["vel0"]).max() < 1e-6 * np.abs(f["vel0"]).max()
+
+
+# ---- the arithmetic the device initial conditions rely on (pm_ics.cu), checked on the host
+
+PCG_MULT = 0x2360ED051FC65DA44385DF649FCCF645
+M128 = (1 << 128) - 1
+
+
+def pcg_advance(state, inc, delta):
+    """Jump-ahead of the 128-bit LCG state' = state * M + inc by delta steps."""
+    cur_mult, cur_plus, acc_mult, acc_plus = PCG_MULT, inc, 1, 0
+    while delta > 0:
+        if delta & 1:
+            acc_mult = (acc_mult * cur_mult) & M128
+            acc_plus = (acc_plus * cur_mult + cur_plus) & M128
+        cur_plus = ((cur_mult + 1) * cur_plus) & M128
+        cur_mult = (cur_mult * cur_mult) & M128
+        delta >>= 1
+    return (acc_mult * state + acc_plus) & M128
+
+
+def xsl_rr(s):
+    x = ((s >> 64) ^ s) & ((1 << 64) - 1)
+    rot = s >> 122
+    return ((x >> rot) | (x << ((64 - rot) & 63))) & ((1 << 64) - 1)
+
+
+@pytest.mark.parametrize("seed", [0, 3, 38, 2 ** 31 - 5])
+def test_pcg64_jump_matches_numpy_jitter_stream(seed):
+    """Draw j of Generator(PCG64(seed)).uniform(-2, 2) = -2 + 4 * (xsl_rr(state after j + 1
+    steps) >> 11) * 2^-53 -- the formula k_zeld_particles evaluates per particle."""
+    from pmgpu.ics import jitter_state
+    (sh, sl), (ih, il) = jitter_state(seed)
+    state, inc = (sh << 64) | sl, (ih << 64) | il
+    draws = np.random.Generator(np.random.PCG64(seed)).uniform(-2.0, 2.0, 5000)
+    for j in (0, 1, 2, 7, 8, 9, 999, 4095, 4999):
+        s = pcg_advance(state, inc, j)
+        s = (s * PCG_MULT + inc) & M128
+        val = -2.0 + 4.0 * ((xsl_rr(s) >> 11) * (1.0 / 9007199254740992.0))
+        assert val == draws[j], (seed, j)
+
+
+def test_uniform_pairs_feed_the_host_box_muller():
+    from pmgpu import ics
+    u, v = ics.uniform_pairs(8, 5)
+    assert u.dtype == np.float32 and u.shape == (512,)
+    s = u.astype(np.float64) ** 2 + v.astype(np.float64) ** 2
+    assert np.all((s > 0) & (s < 1))
+    f1, f2 = ics.gaussian_random_numbers(8, 5)
+    t = -2 * np.log(u ** 2 + v ** 2) / (u ** 2 + v ** 2)
+    assert np.allclose(f1.ravel(), u * t ** 0.5, rtol=1e-6)
+
+
+def test_real_part_of_inverse_fft_is_inverse_rfft_of_hermitian_part():
+    """Re(ifftn(X)) = irfftn of (X[k] + conj(X[-k])) / 2 on the half spectrum (the GRF fill)."""
+    rng = np.random.default_rng(1)
+    n = 12
+    x = rng.standard_normal((n,) * 3) + 1j * rng.standard_normal((n,) * 3)
+    neg = x[np.ix_(*[(-np.arange(n)) % n] * 3)]
+    herm = 0.5 * (x + np.conj(neg))
+    ref = np.fft.ifftn(x).real
+    got = np.fft.irfftn(herm[:, :, : n // 2 + 1], s=(n,) * 3, axes=(0, 1, 2))
+    assert np.allclose(got, ref, atol=1e-12)
+
+
+@pytest.mark.parametrize("direction", [0, 1, 2])
+def test_displacement_spectrum_drops_the_nyquist_plane(direction):
+    """Re(ifftn(-i l_d pot_k)) of a real field = irfftn of i l_d rho_k / |l|^2 with the plane
+    where axis `direction` is at the Nyquist index set to zero (k_zeld_spectrum)."""
+    rng = np.random.default_rng(2)
+    n = 8
+    rho = rng.standard_normal((n,) * 3)
+    ax = 2 * np.pi * np.fft.fftfreq(n)
+    lz, ly, lx = np.meshgrid(ax, ax, ax, indexing="ij")
+    l2 = lx ** 2 + ly ** 2 + lz ** 2
+    rk = np.fft.fftn(rho)
+    pot = np.zeros_like(rk)
+    np.divide(rk, -l2, out=pot, where=l2 != 0)
+    ld = (lz, ly, lx)[direction]
+    ref = np.fft.ifftn(-1j * ld * pot).real
+    half = np.fft.rfftn(rho)
+    lh = [a[:, :, : n // 2 + 1] for a in (lz, ly, lx)]
+    l2h = lh[0] ** 2 + lh[1] ** 2 + lh[2] ** 2
+    g = np.zeros_like(l2h)
+    np.divide(lh[direction], l2h, out=g, where=l2h != 0)
+    idx = [slice(None)] * 3
+    idx[direction] = n // 2
+    g[tuple(idx)] = 0.0
+    got = np.fft.irfftn(1j * g * half, s=(n,) * 3, axes=(0, 1, 2))
+    assert np.allclose(got, ref, atol=1e-12)
