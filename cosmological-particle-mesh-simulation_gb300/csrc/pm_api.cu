@@ -14,6 +14,8 @@ struct pm_ctx {
   const void* maps_for = nullptr;     // spectrum the device tensor maps describe
   DBuf row_start, spec, phi, rho;     // scratch grids
   DBuf hpos, hvel;                    // device copies for pm_step_host
+  DBuf pk_partial, pk_out;            // power spectrum scratch
+  std::vector<double> pk_host;
   std::string err;
 };
 
@@ -239,6 +241,8 @@ void pm_ctx_destroy(pm_ctx* c) {
   c->rho.release();
   c->hpos.release();
   c->hvel.release();
+  c->pk_partial.release();
+  c->pk_out.release();
   delete c;
 }
 
@@ -415,6 +419,46 @@ int pm_sort_keys(pm_ctx* c, const float* positions, long long np, unsigned* keys
   const size_t b = (size_t)np * sizeof(unsigned);
   if (sorted_keys) PM_CK(cudaMemcpyAsync(sorted_keys, skeys, b, cudaMemcpyDeviceToDevice, st), "copy keys");
   if (perm_out) PM_CK(cudaMemcpyAsync(perm_out, perm, b, cudaMemcpyDeviceToDevice, st), "copy perm");
+  return PM_OK;
+}
+
+int pm_power_spectrum(pm_ctx* c, const float* rho, double box_size, int nbins, double* k_out, double* pk_out,
+                      double* modes_out, void* stream) {
+  if (!c) return PM_ERR_ARG;
+  if (!rho || !k_out || !pk_out || !modes_out) return fail(c, PM_ERR_ARG, "null array");
+  const int n = c->n;
+  if (nbins <= 0) nbins = n / 2 + 1;
+  if (nbins < 2 || nbins > n / 2 + 1) return fail(c, PM_ERR_ARG, "nbins must lie in [2, n/2 + 1]");
+  if (!(box_size > 0.0)) return fail(c, PM_ERR_ARG, "box size must be positive");
+  cudaStream_t st = (cudaStream_t)stream;
+  Call k;
+  k.sim = base_sim(c, 1);
+  k.sim.rho = const_cast<float*>(rho);
+  set_prefix(k, 1, n);
+  if (int r = prepare_spectral(c, k)) return r;
+  if (int r = upload(c, k, st)) return r;
+  const Sim* ds = c->d_sim.as<Sim>();
+  const int gx = grid_for(k.prefix[PH_X][1], c->sms, 8), gl = grid_for(k.prefix[PH_LINE][1], c->sms, 8);
+  const CUtensorMap* maps = c->maps_for ? c->d_maps.as<CUtensorMap>() : nullptr;
+  int* err = c->d_err.as<int>();
+  PM_CK(spectral_dispatch(SPEC_X_R2C, n, ds, work(c, k, PH_X), gx, st, maps, err), "x r2c");
+  PM_CK(spectral_dispatch(SPEC_Y_FWD, n, ds, work(c, k, PH_LINE), gl, st, maps, err), "y fwd");
+  PM_CK(spectral_dispatch(SPEC_Z_FWD, n, ds, work(c, k, PH_LINE), gl, st, maps, err), "z fwd");
+  const int nb = nbins - 1;
+  PM_CK(c->pk_partial.ensure(pk_partial_doubles(nbins) * sizeof(double)), "alloc pk");
+  PM_CK(c->pk_out.ensure((size_t)3 * nb * sizeof(double)), "alloc pk");
+  PM_CK(launch_power_spectrum(c->spec.as<float2>(), n, spec_pitch(n), nbins, box_size, c->pk_partial.as<double>(),
+                              c->pk_out.as<double>(), st),
+        "power spectrum");
+  c->pk_host.resize((size_t)3 * nb);
+  PM_CK(cudaMemcpyAsync(c->pk_host.data(), c->pk_out.p, (size_t)3 * nb * sizeof(double), cudaMemcpyDeviceToHost, st),
+        "d2h pk");
+  PM_CK(cudaStreamSynchronize(st), "sync");
+  for (int b = 0; b < nb; ++b) {
+    k_out[b] = c->pk_host[3 * b];
+    pk_out[b] = c->pk_host[3 * b + 1];
+    modes_out[b] = c->pk_host[3 * b + 2];
+  }
   return PM_OK;
 }
 

@@ -118,6 +118,13 @@ bool deposit_r2c_supported(int n);
 cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const unsigned* perm,
                                  const unsigned* row_start, int mode, int* err, int ctas, cudaStream_t st);
 
+// shell-averaged power spectrum of a half spectrum (pm_pk.cu): out = (k, P, modes) for bins
+// 1 .. nbins - 1; nbins <= n / 2 + 1; partial holds pk_partial_doubles(nbins) doubles
+int pk_ctas();
+size_t pk_partial_doubles(int nbins);
+cudaError_t launch_power_spectrum(const float2* spec, int n, int pitch, int nbins, double box, double* partial,
+                                  double* out, cudaStream_t st);
+
 // particle kernels
 cudaError_t launch_keys_abs(const Sim* sims, const Work& w, Parts p, unsigned* keys, unsigned* vals,
                             int* err, int ctas, cudaStream_t st);

@@ -109,6 +109,19 @@ class PMContext:
                                            _stream_ptr()))
         return phi
 
+    def power_spectrum(self, density: torch.Tensor, box_size: float | None = None, nbins: int = 0):
+        """Shell-averaged P(k) of a density grid: (k [h/Mpc], P [(Mpc/h)^3], modes) as numpy
+        float64 arrays of nbins - 1 shells (nbins = 0: N/2 + 1).  Same estimator as the
+        oracle's power_spectrum; no counterpart in the reference."""
+        import numpy as np
+        _need(density, "density", (self.n,) * 3)
+        nb = (self.n // 2 + 1 if nbins <= 0 else nbins) - 1
+        k, p, m = (np.zeros(max(nb, 0), dtype=np.float64) for _ in range(3))
+        box = float(self.cfg.box_size if box_size is None else box_size)
+        self._check(self._lib.pm_power_spectrum(self._h, _ptr(density), box, int(nbins), k.ctypes.data,
+                                                p.ctypes.data, m.ctypes.data, _stream_ptr()))
+        return k, p, m
+
     def integrate(self, positions, velocities, a_val, f_a1, da, potentials):
         """integrate.py:15-97 (in place)."""
         _need(positions, "positions")

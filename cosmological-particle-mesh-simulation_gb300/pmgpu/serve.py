@@ -79,6 +79,7 @@ class Result:
     admitted: float
     completed: float
     particle_updates: int
+    pk: tuple | None = None  # (k, P(k), modes) of the final density (pk=True)
 
     @property
     def latency(self) -> float:
@@ -89,7 +90,7 @@ class Server:
     """Runs a request stream against one GPU in real time."""
 
     def __init__(self, mem_cap_bytes: int, ic_workers: int = 8, steps_per_tick: int = 4, device: int = 0,
-                 keep_results: bool = False, device_ics: bool = True):
+                 keep_results: bool = False, device_ics: bool = True, pk: bool = False):
         import torch
         from .batch import Batch
         self.batch = Batch(device=device, mem_cap_bytes=mem_cap_bytes)
@@ -97,6 +98,8 @@ class Server:
         self.device_ics = device_ics
         self._ics = {}  # N_PARTS -> DeviceICs
         self._ic_stream = torch.cuda.Stream(device=device) if device_ics else None
+        self.pk = pk
+        self._ctx = {}  # N_CELLS -> PMContext (density + power spectrum of finished runs)
         self.cap = mem_cap_bytes
         self.steps_per_tick = steps_per_tick
         self.pool = cf.ProcessPoolExecutor(max_workers=ic_workers, mp_context=mp.get_context("spawn"))
@@ -105,9 +108,10 @@ class Server:
 
     def close(self):
         self.pool.shutdown(wait=False, cancel_futures=True)
-        for g in self._ics.values():
+        for g in list(self._ics.values()) + list(self._ctx.values()):
             g.close()
         self._ics.clear()
+        self._ctx.clear()
         self.batch.close()
 
     def _initial_state(self, r: Request, drawn):
@@ -119,6 +123,16 @@ class Server:
         if g is None:
             g = self._ics[r.n_parts] = DeviceICs(r.n_parts, self.device)
         return g.generate(r.config(), uv=drawn, stream=self._ic_stream)
+
+    def _power_spectrum(self, r: Request, sid: int):
+        """P(k) of a finished simulation's final density, on the GPU (pm_power_spectrum)."""
+        from .context import PMContext
+        cfg = r.config()
+        ctx = self._ctx.get(cfg.n_cells)
+        if ctx is None:
+            ctx = self._ctx[cfg.n_cells] = PMContext(cfg, self.device)
+        pos = self.batch.get(sid, device=True)[0]
+        return ctx.power_spectrum(ctx.density(pos, cfg.mass), box_size=r.box)
 
     def run(self, stream: list[Request], time_limit: float | None = None) -> list[Result]:
         from .batch import Batch
@@ -171,8 +185,9 @@ class Server:
                         r, ta = active.pop(sid)
                         if self.keep_results:
                             self.outputs[r.rid] = self.batch.get(sid)[:2]
+                        pk = self._power_spectrum(r, sid) if self.pk else None
                         self.batch.remove(sid)
-                        results.append(Result(r.rid, r.arrival, ta, now(), r.particle_updates))
+                        results.append(Result(r.rid, r.arrival, ta, now(), r.particle_updates, pk))
             else:
                 time.sleep(0.001)
         self.batch.check_device()

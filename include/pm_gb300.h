@@ -111,6 +111,15 @@ double pm_cosmo_f(double a, double om, double ol, double ok);
 int pm_sort_keys(pm_ctx* ctx, const float* positions, long long np, unsigned* keys_out,
                  unsigned* sorted_keys, unsigned* perm, void* stream);
 
+/* Matter power spectrum of a density grid (no counterpart in the reference; the
+   accuracy statistic of a run): delta = rho / mean(rho) - 1, P(k) = <|delta_k|^2> box^3 / N^6
+   averaged over integer shells b = floor(|m| + 0.5) of the mode index m, 0 < b < nbins
+   (nbins <= N/2 + 1; 0 selects N/2 + 1); rfft modes with 0 < kx < N/2 count twice.
+   Writes nbins - 1 entries to each HOST array: shell k (h/Mpc, the mean |k| of its modes),
+   P(k) ((Mpc/h)^3) and the weighted mode count.  Deterministic; returns after completion. */
+int pm_power_spectrum(pm_ctx* ctx, const float* rho, double box_size, int nbins, double* k_out,
+                      double* pk_out, double* modes_out, void* stream);
+
 /* The CIC deposit of pm_density for callers that cannot allocate device memory (code
    running during stream capture, memory carved up by an arena, latency-critical loops).
    No counterpart in the reference.  All scratch lives in one static device array of the

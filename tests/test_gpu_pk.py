@@ -104,3 +104,70 @@ def test_pk_after_full_run_256p_512g(cuda):
     print("P(k) 256^3/512^3:", {k: v for k, v in res.items() if not isinstance(v, list)})
     assert res["pk_max_rel_dev"] < PK_TOL
     assert res["mass_rel_err"] < 1e-6
+
+
+# ---- the device estimator (pm_power_spectrum) against the oracle's -------------------------
+
+@pytest.mark.parametrize("name", ["n16_g32", "n24_g48", "n32_g64"])
+def test_device_power_spectrum_matches_oracle(cuda, name):
+    torch = cuda
+    from oracle import pm_oracle as O
+    from pmgpu.context import PMContext
+    from conftest import golden_config
+    f, c = load_golden(name)
+    cfg = golden_config(c)
+    rho = f["rho0"]
+    ctx = PMContext(cfg)
+    k, p, m = ctx.power_spectrum(torch.from_numpy(rho).cuda())
+    k2, p2, m2 = O.power_spectrum(rho, cfg.box_size)
+    assert np.array_equal(m, m2)
+    assert np.allclose(k, k2, rtol=1e-12)
+    assert np.abs(p / p2 - 1).max() < 1e-5
+    # deterministic, and a reduced bin count is the prefix of the full one
+    k3, p3, _ = ctx.power_spectrum(torch.from_numpy(rho).cuda())
+    assert np.array_equal(p, p3) and np.array_equal(k, k3)
+    kb, pb, mb = ctx.power_spectrum(torch.from_numpy(rho).cuda(), nbins=cfg.n_cells // 4)
+    assert len(pb) == cfg.n_cells // 4 - 1
+    assert np.array_equal(mb, m[: len(mb)])
+    assert np.allclose(pb, p[: len(pb)], rtol=1e-12)
+    ctx.close()
+
+
+@pytest.mark.parametrize("n_parts,n_cells", [(64, 128), (128, 256), (256, 512)])
+def test_device_power_spectrum_of_evolved_grid(cuda, n_parts, n_cells):
+    """A deposited density after some steps (strongly non-Gaussian) at larger sizes: the
+    float32 spectrum gives P(k) within 1e-4 of the float64 oracle on the same grid."""
+    torch = cuda
+    from oracle import torch64 as T
+    from pmgpu import ics
+    from pmgpu.batch import Batch
+    from pmgpu.config import Config
+    from pmgpu.context import PMContext
+    cfg = Config(n_parts=n_parts, n_cells=n_cells, box_size=150.0, random_seed=2, steps=60)
+    b = Batch()
+    sid = b.add(cfg, *ics.initial_conditions(cfg))
+    b.step(40)
+    pos, _, _, _ = b.get(sid, device=True)
+    b.close()
+    ctx = PMContext(cfg)
+    rho = ctx.density(pos, cfg.mass)
+    k, p, m = ctx.power_spectrum(rho)
+    k2, p2, m2 = T.power_spectrum(rho.double(), cfg.box_size)
+    assert np.array_equal(m, m2)
+    assert np.allclose(k, k2, rtol=1e-12)
+    assert np.abs(p / p2 - 1).max() < 1e-4
+    ctx.close()
+
+
+def test_device_power_spectrum_rejects_bad_arguments(cuda):
+    torch = cuda
+    from pmgpu import _lib
+    from pmgpu.config import Config
+    from pmgpu.context import PMContext
+    ctx = PMContext(Config(n_parts=16, n_cells=32))
+    rho = torch.ones((32,) * 3, device="cuda")
+    with pytest.raises(_lib.PMError):
+        ctx.power_spectrum(rho, nbins=40)
+    with pytest.raises(_lib.PMError):
+        ctx.power_spectrum(rho, box_size=-1.0)
+    ctx.close()

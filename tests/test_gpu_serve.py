@@ -18,7 +18,8 @@ def test_served_results_equal_alone(cuda, device_ics):
               Request(4, 15, 12, 120.0, 25, 0.15), Request(5, 16, 32, 300.0, 15, 0.2)]
     # a cap that holds about two of the larger requests: later ones wait for memory
     cap = 2 * Batch.footprint(stream[2].config()) + Batch.footprint(stream[0].config())
-    srv = Server(mem_cap_bytes=cap, ic_workers=2, steps_per_tick=3, keep_results=True, device_ics=device_ics)
+    srv = Server(mem_cap_bytes=cap, ic_workers=2, steps_per_tick=3, keep_results=True, device_ics=device_ics,
+                 pk=device_ics)
     res = srv.run(stream)
     srv.close()
     assert sorted(r.rid for r in res) == list(range(len(stream)))
@@ -36,3 +37,12 @@ def test_served_results_equal_alone(cuda, device_ics):
         b.close()
         pm, vm = srv.outputs[r.rid]
         assert np.array_equal(p, pm) and np.array_equal(v, vm)
+    if device_ics:  # every result carries the power spectrum of its final density
+        from oracle import pm_oracle as O
+        for out in res:
+            r = stream[out.rid]
+            k, pk, modes = out.pk
+            pos = srv.outputs[out.rid][0]
+            rho = O.density(pos, r.config().mass, r.config().n_cells)
+            k2, pk2, m2 = O.power_spectrum(rho, r.box)
+            assert np.array_equal(modes, m2) and np.abs(pk / pk2 - 1).max() < 1e-4
