@@ -422,6 +422,16 @@ int pm_sort_keys(pm_ctx* c, const float* positions, long long np, unsigned* keys
   return PM_OK;
 }
 
+int pm_project(pm_ctx* c, const float* rho, int n_slices, double* out, void* stream) {
+  if (!c) return PM_ERR_ARG;
+  if (!rho || !out) return fail(c, PM_ERR_ARG, "null array");
+  if (n_slices < 0 || n_slices > c->n) return fail(c, PM_ERR_ARG, "n_slices must lie in [0, N]");
+  const long long plane = (long long)c->n * c->n;
+  PM_CK(launch_project(rho, c->n, n_slices, out, grid_for((plane + 255) / 256, c->sms, 8), (cudaStream_t)stream),
+        "project");
+  return PM_OK;
+}
+
 int pm_power_spectrum(pm_ctx* c, const float* rho, double box_size, int nbins, double* k_out, double* pk_out,
                       double* modes_out, void* stream) {
   if (!c) return PM_ERR_ARG;

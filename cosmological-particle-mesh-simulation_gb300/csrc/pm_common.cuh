@@ -118,7 +118,9 @@ bool deposit_r2c_supported(int n);
 cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const unsigned* perm,
                                  const unsigned* row_start, int mode, int* err, int ctas, cudaStream_t st);
 
-// shell-averaged power spectrum of a half spectrum (pm_pk.cu): out = (k, P, modes) for bins
+// sum of the first n_slices planes of an n^3 grid, float64 n^2 output (pm_diagnostics.cu)
+cudaError_t launch_project(const float* rho, int n, int n_slices, double* out, int ctas, cudaStream_t st);
+// shell-averaged power spectrum of a half spectrum (pm_diagnostics.cu): out = (k, P, modes) for bins
 // 1 .. nbins - 1; nbins <= n / 2 + 1; partial holds pk_partial_doubles(nbins) doubles
 int pk_ctas();
 size_t pk_partial_doubles(int nbins);

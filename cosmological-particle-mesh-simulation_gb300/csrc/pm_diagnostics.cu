@@ -1,4 +1,7 @@
-// Matter power spectrum of a density grid from its half spectrum: shell-averaged
+// Diagnostics of a density grid: the slab projection of plot_helper.py:65-72 and the matter
+// power spectrum.
+//
+// Power spectrum, from the grid's half spectrum: shell-averaged
 // P(k) = <|delta_k|^2> box^3 / n^6 in integer shells of |m| (m: mode index), delta = rho /
 // mean(rho) - 1.  The reference has no estimator; this one has the binning of the oracle's
 // power_spectrum: bin b = floor(|m| + 0.5) for 0 < b < nbins, modes with 0 < kx < n/2
@@ -104,7 +107,24 @@ __global__ void k_pk_final(const double* __restrict__ partial, int ctas, int nbi
   o[2] = c;
 }
 
+// plot_helper.py:65-72: out[y][x] = sum over i < n_slices of rho[i][y][x], in float64 and
+// in plane order (as the reference's loop).  One thread per (y, x): reads are coalesced.
+__global__ void k_project(const float* __restrict__ rho, int n, int n_slices, double* __restrict__ out) {
+  const long long plane = (long long)n * n;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < plane;
+       e += (long long)gridDim.x * blockDim.x) {
+    double t = 0.0;
+    for (int i = 0; i < n_slices; ++i) t += (double)__ldg(&rho[i * plane + e]);
+    out[e] = t;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_project(const float* rho, int n, int n_slices, double* out, int ctas, cudaStream_t st) {
+  k_project<<<ctas, 256, 0, st>>>(rho, n, n_slices, out);
+  return cudaGetLastError();
+}
 
 int pk_ctas() { return 256; }
 

@@ -62,6 +62,11 @@ def _resident(positions, velocities, a_current, da, da_save, n_file):
     cfg.steps = max(1, int(round((A_END - a_current) / da)))
     b = Batch()
     sid = b.add(cfg, positions, velocities)
+    writer = None
+    if SAVE_DATA:  # snapshots are copied out and written while the next steps run
+        from pmgpu.snapshot import SnapshotWriter
+        from save_data import DATA_DIR
+        writer = SnapshotWriter(BOX_SIZE, N_CELLS, H0, directory=DATA_DIR)
     print("Starting the integrations (resident on the GPU)...")
     while b.active(sid):
         start_time = time()
@@ -72,13 +77,15 @@ def _resident(positions, velocities, a_current, da, da_save, n_file):
         b.step(k)
         a, done = b.state(sid)
         if SAVE_DATA and a >= target:
-            positions, velocities, _, _ = b.get(sid)
-            save_file(None, positions, velocities, n_file, a)
+            pos_d, vel_d, _, _ = b.get(sid, device=True)
+            writer.submit(n_file, pos_d, vel_d, a)
             n_file += 1
         if PRINT_STATUS:
             print_status(a, start_time)
     b.check_device()
     positions, velocities, _, _ = b.get(sid)
+    if writer is not None:
+        writer.close()
     return positions, velocities
 
 

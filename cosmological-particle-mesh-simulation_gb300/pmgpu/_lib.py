@@ -50,6 +50,7 @@ SIGNATURES = {
     "pm_step_host": (c_int, [c_void_p, c_void_p, c_void_p, c_ll, c_double, c_double, c_double, c_void_p]),
     "pm_cosmo_f": (c_double, [c_double, c_double, c_double, c_double]),
     "pm_sort_keys": (c_int, [c_void_p, c_void_p, c_ll, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pm_project": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
     "pm_power_spectrum": (c_int, [c_void_p, c_void_p, c_double, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "pm_density_noalloc": (c_int, [c_void_p, c_ll, c_int, c_double, c_void_p, c_void_p]),
     "pm_ics_create": (c_int, [c_int, c_int, ctypes.POINTER(c_void_p)]),

@@ -24,7 +24,7 @@ LIB = os.path.join(PKG, "libpm_gb300.so")
 GRID_SIZES = (16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024)
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 SOURCES = ("pm_api.cu", "pm_batch.cu", "pm_particles.cu", "pm_sort.cu", "pm_spectral_host.cu", "pm_noalloc.cu",
-           "pm_ics.cu", "pm_pk.cu")
+           "pm_ics.cu", "pm_diagnostics.cu")
 
 
 def _nvcc():

@@ -109,6 +109,13 @@ class PMContext:
                                            _stream_ptr()))
         return phi
 
+    def project(self, density: torch.Tensor, n_slices: int) -> torch.Tensor:
+        """plot_helper.py:65-72: sum of the first n_slices planes, float64 (N, N)."""
+        _need(density, "density", (self.n,) * 3)
+        out = torch.empty((self.n, self.n), dtype=torch.float64, device=density.device)
+        self._check(self._lib.pm_project(self._h, _ptr(density), int(n_slices), _ptr(out), _stream_ptr()))
+        return out
+
     def power_spectrum(self, density: torch.Tensor, box_size: float | None = None, nbins: int = 0):
         """Shell-averaged P(k) of a density grid: (k [h/Mpc], P [(Mpc/h)^3], modes) as numpy
         float64 arrays of nbins - 1 shells (nbins = 0: N/2 + 1).  Same estimator as the

@@ -111,6 +111,10 @@ double pm_cosmo_f(double a, double om, double ol, double ok);
 int pm_sort_keys(pm_ctx* ctx, const float* positions, long long np, unsigned* keys_out,
                  unsigned* sorted_keys, unsigned* perm, void* stream);
 
+/* src/plot_helper.py:65-72  project(rho, n_slices): out[y][x] = sum of rho[i][y][x] over the
+   first n_slices planes (float64, N x N, device). */
+int pm_project(pm_ctx* ctx, const float* rho, int n_slices, double* out, void* stream);
+
 /* Matter power spectrum of a density grid (no counterpart in the reference; the
    accuracy statistic of a run): delta = rho / mean(rho) - 1, P(k) = <|delta_k|^2> box^3 / N^6
    averaged over integer shells b = floor(|m| + 0.5) of the mode index m, 0 < b < nbins

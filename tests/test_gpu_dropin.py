@@ -12,7 +12,7 @@ from conftest import load_golden, periodic_maxdiff, rel_l2
 pytestmark = pytest.mark.gpu
 
 DROPIN = ["configure_me", "density", "fourier_utils", "potential", "integrate", "cosmology",
-          "gaussian_random_field", "zeldovich", "save_data", "pmesh"]
+          "gaussian_random_field", "zeldovich", "save_data", "pmesh", "plot_helper"]
 
 
 def install_config(c, **extra):
@@ -81,3 +81,35 @@ def test_pmesh_driver_resident_and_loop_agree(cuda, restore_modules):
     # the resident engine stores displacements (more precise): small differences only
     assert periodic_maxdiff(p0, p1, c["N_CELLS"]) < 5e-3
     assert rel_l2(v0, v1) < 1e-3
+
+
+def test_projection_is_the_reference_loop(cuda, restore_modules):
+    """plot_helper.py:65-72: float64 sum of the first planes, in plane order (bit-identical)."""
+    f, c = load_golden("n32_g64")
+    install_config(c)
+    plot_helper = importlib.import_module("plot_helper")
+    rho = f["rho0"]
+    for n_slices in (0, 1, 15, rho.shape[0]):
+        expect = np.zeros(rho.shape[1:], dtype=np.float64)
+        for i in range(n_slices):
+            expect += rho[i, :, :]
+        got = plot_helper.project(rho, n_slices)
+        assert got.dtype == np.float64 and np.array_equal(got, expect)
+
+
+def test_pmesh_resident_writes_snapshots_in_the_background(cuda, restore_modules, tmp_path, monkeypatch):
+    """SAVE_DATA with the resident engine: snapshot files with the reference's datasets,
+    written by the background writer while the run continues."""
+    from pmgpu.snapshot import read_file
+    f, c = load_golden("n16_g32")
+    c = dict(c, STEPS=20)
+    monkeypatch.chdir(tmp_path)
+    install_config(c, RESIDENT=True, SAVE_DATA=True, N_SAVE_FILES=4)
+    pmesh = importlib.import_module("pmesh")
+    pos, vel = pmesh.simulator()
+    files = sorted(p.name for p in (tmp_path / "Data").iterdir())
+    assert len(files) >= 4 and files[0].startswith("data.0.")
+    last = read_file(str(tmp_path / "Data" / files[-1]))
+    assert set(last) >= {"x1", "x2", "x3", "vx1", "vx2", "vx3", "a"}
+    assert last["x1"].dtype == np.float32 and last["x1"].shape == (c["N_PARTS"] ** 3,)
+    assert np.isfinite(last["vx3"]).all() and 0 < float(last["a"]) <= c["A_END"]

@@ -175,3 +175,20 @@ def test_displacement_spectrum_drops_the_nyquist_plane(direction):
     g[tuple(idx)] = 0.0
     got = np.fft.irfftn(1j * g * half, s=(n,) * 3, axes=(0, 1, 2))
     assert np.allclose(got, ref, atol=1e-12)
+
+
+def test_snapshot_units_and_file_roundtrip(tmp_path):
+    """save_data.py:10-11 conversions and the dataset names; files read back unchanged."""
+    from pmgpu.snapshot import host_snapshot, read_file, units, write_file
+    up, uv = units(0.5, 250.0, 512, 0.7)
+    assert up == 7.8 * (250.0 / (512 / 128)) / 10 ** 3
+    assert uv == 0.781 * 250.0 * 0.7 / (0.5 * 512 / 128)
+    rng = np.random.default_rng(0)
+    pos = rng.uniform(0, 512, (3, 100)).astype(np.float32)
+    vel = rng.standard_normal((3, 100)).astype(np.float32)
+    d = host_snapshot(pos, vel, 0.5, 250.0, 512, 0.7)
+    assert d["x2"].dtype == np.float32 and np.array_equal(d["x2"], pos[1] * up)
+    path = str(tmp_path / "data.3.npz")
+    write_file(path, d)
+    back = read_file(path)
+    assert set(back) == set(d) and all(np.array_equal(back[k], d[k]) for k in d)
