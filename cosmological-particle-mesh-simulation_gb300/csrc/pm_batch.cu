@@ -47,6 +47,7 @@ struct Plan {
   std::vector<int> single;               // per distinct size: the only simulation of that size, or -1
   std::vector<int> fused, fdep_total;    // per distinct size: deposit fused with the x R2C, its tiles
   int max_dep_smem = 0;
+  int max_n = 0;
 };
 
 const int kStateArrays = 7;
@@ -67,6 +68,7 @@ struct pm_batch {
   int cur = 0;
   SortBufs sort;
   DBuf row_start, d_sims, d_prefix, d_err, d_maps;
+  DBuf row_count, row_cursor, scan_sums;  // counting sort of the row keys
   Plan plan;
   bool dirty = true, keys_valid = false;
   bool graphs = true;
@@ -119,7 +121,7 @@ size_t footprint(const pm_config& c) {
   f += n * n * (size_t)spec_pitch((int)n) * sizeof(float2);      // spectrum
   f += np * (2 * kStateArrays * 4 + 4 * 4);                      // state x2, keys/vals x2
   f += np * 6 * sizeof(float);                                   // final state
-  f += n * n * sizeof(unsigned) + 4096;                          // row starts, tables
+  f += 3 * n * n * sizeof(unsigned) + 4096;                      // row starts, counts, cursors, tables
   return f;
 }
 
@@ -179,9 +181,8 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   P.nsims = (int)b->sims.size();
   if (P.nsims == 0) return PM_OK;
   // Resident keys are the global x-row number alone: the deposit needs particles grouped by
-  // row, not ordered inside a row (its integer sums do not depend on the order), and the
-  // stable sort keeps the previous step's order inside each row.  The key space is the
-  // batch's total number of rows (< 2^32).
+  // row, not ordered inside a row (its integer sums do not depend on the order), so a
+  // counting sort over the batch's rows (< 2^32) groups them.
   P.xbits = 0;
   std::vector<Sim> hs(P.nsims);
   const int S = P.nsims;
@@ -251,6 +252,7 @@ int build_plan(pm_batch* b, cudaStream_t st) {
     at(PH_KEYS, i + 1) = at(PH_KEYS, i) + (int)((r.np + 255) / 256);
     at(PH_DEP, i + 1) = at(PH_DEP, i) + (fused_here ? 0 : tiles);
     at(PH_KICK, i + 1) = at(PH_KICK, i) + (int)((r.np + KICK_UNIT - 1) / KICK_UNIT);
+    P.max_n = std::max(P.max_n, r.n);
     for (size_t g = 0; g < P.sizes.size(); ++g) {
       const bool mine = P.sizes[g] == r.n;
       const int phx = PH_FIXED + 3 * (int)g, phl = phx + 1, phd = phx + 2;
@@ -281,6 +283,9 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   PB_CK(b->d_sims.ensure(sizeof(Sim) * S), "alloc sims");
   PB_CK(b->d_prefix.ensure(sizeof(int) * pre.size()), "alloc prefix");
   PB_CK(b->row_start.ensure(sizeof(unsigned) * ((size_t)rows + 1)), "alloc rows");
+  PB_CK(b->row_count.ensure(sizeof(unsigned) * (size_t)rows), "alloc rows");
+  PB_CK(b->row_cursor.ensure(sizeof(unsigned) * (size_t)rows), "alloc rows");
+  PB_CK(b->scan_sums.ensure(sizeof(unsigned) * row_sort_block_sums(rows)), "alloc rows");
   PB_CK(cudaMemcpyAsync(b->d_sims.p, hs.data(), sizeof(Sim) * S, cudaMemcpyHostToDevice, st), "upload sims");
   PB_CK(cudaMemcpyAsync(b->d_prefix.p, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, st),
         "upload prefix");
@@ -319,15 +324,14 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
   const Sim* ds = b->d_sims.as<Sim>();
   int* err = b->d_err.as<int>();
   Parts in = state(b, cur), out = state(b, 1 - cur);
-  bool alt = false;
-  PB_CK(radix_sort(b->sort.keys.as<unsigned>(), b->sort.vals.as<unsigned>(), P.ptot, 0, P.bits, true,
-                   b->sort.scratch(), &alt, st),
+  // group the particles by x-row: row starts and the permutation to row order
+  unsigned* perm = b->sort.vals.as<unsigned>();
+  PB_CK(row_counting_sort(b->sort.keys.as<unsigned>(), P.ptot, P.rows, b->row_count.as<unsigned>(),
+                          b->row_start.as<unsigned>(), b->row_cursor.as<unsigned>(), b->scan_sums.as<unsigned>(),
+                          perm, err, b->sms, st),
         "sort");
-  unsigned* perm = alt ? b->sort.vals_alt.as<unsigned>() : b->sort.vals.as<unsigned>();
-  unsigned* skeys = alt ? b->sort.keys_alt.as<unsigned>() : b->sort.keys.as<unsigned>();
   PB_CK(mark(1 + PP_SORT), "event");
-  PB_CK(launch_row_start(skeys, P.ptot, P.xbits, P.rows, b->row_start.as<unsigned>(), st), "rows");
-  PB_CK(mark(1 + PP_ROWS), "event");
+  PB_CK(mark(1 + PP_ROWS), "event");  // the row starts come out of the counting sort
   if (P.fixed_total[PH_DEP] > 0)
     PB_CK(launch_deposit(ds, work_of(b, PH_DEP, P.fixed_total[PH_DEP]), in, perm, b->row_start.as<unsigned>(),
                          POS_DISP, err, grid_for(P.fixed_total[PH_DEP], b->sms, 3), P.max_dep_smem, st),
@@ -366,8 +370,8 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
 // Kernel launches of one step for the current plan.
 int launches_per_step(pm_batch* b) {
   const Plan& P = b->plan;
-  const int passes = radix_sort_passes(P.bits);
-  int n = 3 * passes + 1 + (P.fixed_total[PH_DEP] > 0 ? 1 : 0) + 5 * (int)P.sizes.size() + 1 + 1;
+  // counting sort: histogram, 3 scan kernels, scatter (the count reset is a memset)
+  int n = 5 + (P.fixed_total[PH_DEP] > 0 ? 1 : 0) + 5 * (int)P.sizes.size() + 1 + 1;
   return n;  // each fused size replaces its x R2C launch by the fused deposit
 }
 
@@ -505,6 +509,9 @@ void pm_batch_destroy(pm_batch* b) {
   for (auto& l : b->lattices) l.second->release();
   b->sort.release();
   b->row_start.release();
+  b->row_count.release();
+  b->row_cursor.release();
+  b->scan_sums.release();
   b->d_sims.release();
   b->d_prefix.release();
   b->d_err.release();

@@ -165,5 +165,13 @@ int radix_sort_passes(int bits);
 // vals are not read on the first pass and the identity 0..n-1 is used instead.
 cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int begin_bit, int bits, bool gen_vals,
                        const SortScratch& s, bool* in_alt, cudaStream_t st);
+// Groups n row keys (< nrows) by row: row_start[0..nrows] (exclusive prefix of the row
+// counts) and perm[j] = index of the j-th key in row order (order inside a row not
+// specified).  Scratch: count and cursor (nrows each), block_sums (row_sort_block_sums).
+size_t row_sort_block_sums(unsigned nrows);
+// inv (optional): inv[i] = sorted position of key i.
+cudaError_t row_counting_sort(const unsigned* keys, long long n, unsigned nrows, unsigned* count,
+                              unsigned* row_start, unsigned* cursor, unsigned* block_sums, unsigned* perm, int* err,
+                              int sms, cudaStream_t st, unsigned* inv = nullptr);
 
 }  // namespace pm

@@ -12,6 +12,7 @@
 // pm_deposit.cuh (shared with the fused deposit + x-transform kernel).
 #include "pm_cells.cuh"
 #include "pm_deposit.cuh"
+#include "pm_tma.cuh"
 
 namespace pm {
 
@@ -104,33 +105,58 @@ __global__ void __launch_bounds__(DEP_NT, 3) k_deposit(const Sim* __restrict__ s
 // POS_DISP: displacements; the particle that is i-th in sorted order is written to
 //          output slot sort_off + i, together with its cell key for the next step.
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ void gather_force(const float* __restrict__ phi, int n, const Cell& c,
-                                             float g[3]) {
+// Potential rows around a particle, read from global memory: row(oy, oz) is the x-row at
+// (y + oy, z + oz) (periodic), oy, oz in {-1, 0, 1, 2}.
+struct GlobalRows {
+  const float* phi;
+  int n, ys[4], zs[4];  // y - 1, y, y + 1, y + 2 and the same for z, wrapped
+  __device__ __forceinline__ GlobalRows(const float* p, int nn, int y, int z) : phi(p), n(nn) {
+    ys[1] = y; ys[0] = y == 0 ? n - 1 : y - 1; ys[2] = y + 1 == n ? 0 : y + 1; ys[3] = ys[2] + 1 == n ? 0 : ys[2] + 1;
+    zs[1] = z; zs[0] = z == 0 ? n - 1 : z - 1; zs[2] = z + 1 == n ? 0 : z + 1; zs[3] = zs[2] + 1 == n ? 0 : zs[2] + 1;
+  }
+  __device__ __forceinline__ const float* row(int oy, int oz) const {
+    return phi + (size_t)(unsigned)(zs[oz + 1] * n + ys[oy + 1]) * (unsigned)n;
+  }
+  __device__ __forceinline__ float ld(const float* p) const { return __ldg(p); }
+};
+
+// The same rows from the shared-memory block of a kick tile: (TZ + 3) x (TY + 3) rows
+// starting at (y0 - 1, z0 - 1); (dy, dz) = base cell - tile origin.
+struct SharedRows {
+  const float* s;
+  int n, dy, dz;
+  __device__ __forceinline__ const float* row(int oy, int oz) const {
+    return s + ((dz + 1 + oz) * (TY + 3) + (dy + 1 + oy)) * n;
+  }
+  __device__ __forceinline__ float ld(const float* p) const { return *p; }
+};
+
+// integrate.py:54-97: the 32 potential taps of the three finite-difference gradients at the
+// 8 CIC corners, combined with the CIC weights in the reference's order.
+template <class ROWS>
+__device__ __forceinline__ void gather_taps(const ROWS& R, int n, const Cell& c, float g[3]) {
   float w[8];
   cic_weights(c, w);
   const int xm = c.x == 0 ? n - 1 : c.x - 1, x1 = c.x + 1 == n ? 0 : c.x + 1, x2 = x1 + 1 == n ? 0 : x1 + 1;
-  const int ym = c.y == 0 ? n - 1 : c.y - 1, y1 = c.y + 1 == n ? 0 : c.y + 1, y2 = y1 + 1 == n ? 0 : y1 + 1;
-  const int zm = c.z == 0 ? n - 1 : c.z - 1, z1 = c.z + 1 == n ? 0 : c.z + 1, z2 = z1 + 1 == n ? 0 : z1 + 1;
-  const int x0 = c.x, y0 = c.y, z0 = c.z;
+  const int x0 = c.x;
   // the 12 x-rows the 32 taps lie in
-  auto row = [&](int y, int z) { return phi + (size_t)(unsigned)(z * n + y) * (unsigned)n; };
-  const float* r00 = row(y0, z0); const float* r10 = row(y1, z0);
-  const float* r01 = row(y0, z1); const float* r11 = row(y1, z1);
-  const float* rm0 = row(ym, z0); const float* rm1 = row(ym, z1);
-  const float* r20 = row(y2, z0); const float* r21 = row(y2, z1);
-  const float* r0m = row(y0, zm); const float* r1m = row(y1, zm);
-  const float* r02 = row(y0, z2); const float* r12 = row(y1, z2);
+  const float* r00 = R.row(0, 0); const float* r10 = R.row(1, 0);
+  const float* r01 = R.row(0, 1); const float* r11 = R.row(1, 1);
+  const float* rm0 = R.row(-1, 0); const float* rm1 = R.row(-1, 1);
+  const float* r20 = R.row(2, 0); const float* r21 = R.row(2, 1);
+  const float* r0m = R.row(0, -1); const float* r1m = R.row(1, -1);
+  const float* r02 = R.row(0, 2); const float* r12 = R.row(1, 2);
   // x gradient taps: rows (y0|y1, z0|z1) at xm, x0, x1, x2   (naming a<y><z><x>)
-  const float a00m = __ldg(r00 + xm), a000 = __ldg(r00 + x0), a001 = __ldg(r00 + x1), a002 = __ldg(r00 + x2);
-  const float a10m = __ldg(r10 + xm), a100 = __ldg(r10 + x0), a101 = __ldg(r10 + x1), a102 = __ldg(r10 + x2);
-  const float a01m = __ldg(r01 + xm), a010 = __ldg(r01 + x0), a011 = __ldg(r01 + x1), a012 = __ldg(r01 + x2);
-  const float a11m = __ldg(r11 + xm), a110 = __ldg(r11 + x0), a111 = __ldg(r11 + x1), a112 = __ldg(r11 + x2);
+  const float a00m = R.ld(r00 + xm), a000 = R.ld(r00 + x0), a001 = R.ld(r00 + x1), a002 = R.ld(r00 + x2);
+  const float a10m = R.ld(r10 + xm), a100 = R.ld(r10 + x0), a101 = R.ld(r10 + x1), a102 = R.ld(r10 + x2);
+  const float a01m = R.ld(r01 + xm), a010 = R.ld(r01 + x0), a011 = R.ld(r01 + x1), a012 = R.ld(r01 + x2);
+  const float a11m = R.ld(r11 + xm), a110 = R.ld(r11 + x0), a111 = R.ld(r11 + x1), a112 = R.ld(r11 + x2);
   // y extension rows ym, y2 at x0, x1 (z0, z1)
-  const float bm00 = __ldg(rm0 + x0), bm01 = __ldg(rm0 + x1), b200 = __ldg(r20 + x0), b201 = __ldg(r20 + x1);
-  const float bm10 = __ldg(rm1 + x0), bm11 = __ldg(rm1 + x1), b210 = __ldg(r21 + x0), b211 = __ldg(r21 + x1);
+  const float bm00 = R.ld(rm0 + x0), bm01 = R.ld(rm0 + x1), b200 = R.ld(r20 + x0), b201 = R.ld(r20 + x1);
+  const float bm10 = R.ld(rm1 + x0), bm11 = R.ld(rm1 + x1), b210 = R.ld(r21 + x0), b211 = R.ld(r21 + x1);
   // z extension planes zm, z2 at (x0|x1, y0|y1)
-  const float cm00 = __ldg(r0m + x0), cm01 = __ldg(r0m + x1), cm10 = __ldg(r1m + x0), cm11 = __ldg(r1m + x1);
-  const float c200 = __ldg(r02 + x0), c201 = __ldg(r02 + x1), c210 = __ldg(r12 + x0), c211 = __ldg(r12 + x1);
+  const float cm00 = R.ld(r0m + x0), cm01 = R.ld(r0m + x1), cm10 = R.ld(r1m + x0), cm11 = R.ld(r1m + x1);
+  const float c200 = R.ld(r02 + x0), c201 = R.ld(r02 + x1), c210 = R.ld(r12 + x0), c211 = R.ld(r12 + x1);
   // x axis: g(o) = phi[x+ox-1] - phi[x+ox+1]   (corner naming g<ox><oy><oz>)
   const float gx000 = a00m - a001, gx100 = a000 - a002;
   const float gx010 = a10m - a101, gx110 = a100 - a102;
@@ -153,6 +179,10 @@ __device__ __forceinline__ void gather_force(const float* __restrict__ phi, int 
           gy011 * w[6] + gy111 * w[7]) * 0.5f;
   g[2] = (gz000 * w[0] + gz100 * w[1] + gz010 * w[2] + gz001 * w[3] + gz110 * w[4] + gz101 * w[5] +
           gz011 * w[6] + gz111 * w[7]) * 0.5f;
+}
+
+__device__ __forceinline__ void gather_force(const float* __restrict__ phi, int n, const Cell& c, float g[3]) {
+  gather_taps(GlobalRows(phi, n, c.y, c.z), n, c, g);
 }
 
 // Kick/drift of one particle whose state and force are in registers; writes it out.

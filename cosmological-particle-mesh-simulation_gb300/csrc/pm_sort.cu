@@ -249,4 +249,152 @@ cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int begin_bi
   return cudaSuccess;
 }
 
+
+
+// ---------------------------------------------------------------------------------
+// Counting sort of row keys (resident batches).  The deposit and the kick need the
+// particles grouped by x-row, not ordered inside a row: a histogram of the rows, its
+// exclusive scan (the row starts) and one scatter through per-row cursors replace the
+// radix passes.  The order inside a row depends on the scheduling of the cursor atomics;
+// nothing downstream depends on it (the deposit sums integers, the kick is per particle).
+// Equal keys of a warp are combined by a match first (the state is nearly sorted, so a
+// warp touches few rows).
+// ---------------------------------------------------------------------------------
+namespace {
+
+constexpr int CS_NT = 256;
+constexpr int SCAN_TILE = 4096;  // rows per block of the row-start scan
+constexpr int SCAN_IPT = SCAN_TILE / CS_NT;
+
+__global__ void __launch_bounds__(CS_NT) k_row_hist(const unsigned* __restrict__ keys, long long n, unsigned nrows,
+                                                    unsigned* __restrict__ count, int* err) {
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * CS_NT;
+  for (long long b = (long long)blockIdx.x * CS_NT + (threadIdx.x & ~31); b < n; b += stride) {
+    const long long i = b + lane;
+    unsigned k = i < n ? __ldg(&keys[i]) : 0xffffffffu;
+    if (i < n && k >= nrows) {
+      set_error(err, ERR_CELL_RANGE);
+      k = nrows - 1;
+    }
+    const unsigned grp = __match_any_sync(0xffffffffu, k);
+    if (k != 0xffffffffu && lane == __ffs(grp) - 1) atomicAdd(&count[k], (unsigned)__popc(grp));
+  }
+}
+
+// per-block sums of SCAN_TILE entries
+__global__ void __launch_bounds__(CS_NT) k_scan_reduce(const unsigned* __restrict__ in, long long n,
+                                                       unsigned* __restrict__ block_sums) {
+  __shared__ unsigned ws[CS_NT / 32];
+  const long long base = (long long)blockIdx.x * SCAN_TILE;
+  unsigned s = 0;
+#pragma unroll
+  for (int j = 0; j < SCAN_IPT; ++j) {
+    const long long i = base + j * CS_NT + threadIdx.x;
+    if (i < n) s += __ldg(&in[i]);
+  }
+  unsigned total;
+  block_exclusive_scan<CS_NT>(s, ws, total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// exclusive scan of the block sums in place (one block, chunks of CS_NT with a carry)
+__global__ void __launch_bounds__(CS_NT) k_scan_top(unsigned* __restrict__ block_sums, int nblocks) {
+  __shared__ unsigned ws[CS_NT / 32];
+  unsigned carry = 0;
+  for (int c = 0; c < nblocks; c += CS_NT) {
+    const int i = c + threadIdx.x;
+    const unsigned v = i < nblocks ? block_sums[i] : 0u;
+    unsigned total;
+    const unsigned ex = block_exclusive_scan<CS_NT>(v, ws, total);
+    if (i < nblocks) block_sums[i] = carry + ex;
+    carry += total;
+    __syncthreads();
+  }
+}
+
+// out[i] = exclusive prefix of in, i < n; out[n] = total; cursor = copy of out[0, n)
+__global__ void __launch_bounds__(CS_NT) k_scan_apply(const unsigned* __restrict__ in, long long n,
+                                                      const unsigned* __restrict__ block_sums,
+                                                      unsigned* __restrict__ out, unsigned* __restrict__ cursor) {
+  __shared__ unsigned ws[CS_NT / 32];
+  const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_IPT;
+  unsigned v[SCAN_IPT];
+  unsigned s = 0;
+#pragma unroll
+  for (int j = 0; j < SCAN_IPT; ++j) {
+    const long long i = base + j;
+    v[j] = i < n ? __ldg(&in[i]) : 0u;
+    s += v[j];
+  }
+  unsigned total;
+  unsigned run = block_sums[blockIdx.x] + block_exclusive_scan<CS_NT>(s, ws, total);
+#pragma unroll
+  for (int j = 0; j < SCAN_IPT; ++j) {
+    const long long i = base + j;
+    if (i < n) {
+      out[i] = run;
+      cursor[i] = run;
+    }
+    run += v[j];
+    if (i == n - 1) out[n] = run;
+  }
+}
+
+// Each warp scatters one chunk of SCATTER_CHUNK consecutive keys, in order: the keys of a
+// row that lie in one chunk keep their order and stay together, so a row's range is made
+// of a few ordered runs (one per chunk it spans) and a nearly sorted input stays nearly
+// in place -- the next reads through the permutation remain coalesced.
+constexpr int SCATTER_CHUNK = 1024;
+
+__global__ void __launch_bounds__(CS_NT) k_row_scatter(const unsigned* __restrict__ keys, long long n, unsigned nrows,
+                                                       unsigned* __restrict__ cursor, unsigned* __restrict__ perm,
+                                                       unsigned* __restrict__ inv) {
+  const int lane = threadIdx.x & 31;
+  const long long nchunks = (n + SCATTER_CHUNK - 1) / SCATTER_CHUNK;
+  const long long nwarps = (long long)gridDim.x * (CS_NT / 32);
+  for (long long c = (long long)blockIdx.x * (CS_NT / 32) + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
+    const long long end = (c + 1) * SCATTER_CHUNK < n ? (c + 1) * SCATTER_CHUNK : n;
+    for (long long b = c * SCATTER_CHUNK; b < end; b += 32) {
+      const long long i = b + lane;
+      unsigned k = i < end ? __ldg(&keys[i]) : 0xffffffffu;
+      if (i < end && k >= nrows) k = nrows - 1;
+      const unsigned grp = __match_any_sync(0xffffffffu, k);
+      const int leader = __ffs(grp) - 1;
+      unsigned pos = 0;
+      if (k != 0xffffffffu && lane == leader) pos = atomicAdd(&cursor[k], (unsigned)__popc(grp));
+      pos = __shfl_sync(0xffffffffu, pos, leader);
+      if (k != 0xffffffffu) {
+        const unsigned p = pos + __popc(grp & ((1u << lane) - 1u));
+        perm[p] = (unsigned)i;
+        if (inv) inv[i] = p;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+size_t row_sort_block_sums(unsigned nrows) { return ((size_t)nrows + SCAN_TILE - 1) / SCAN_TILE; }
+
+cudaError_t row_counting_sort(const unsigned* keys, long long n, unsigned nrows, unsigned* count,
+                              unsigned* row_start, unsigned* cursor, unsigned* block_sums, unsigned* perm, int* err,
+                              int sms, cudaStream_t st, unsigned* inv) {
+  if (nrows == 0) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(count, 0, (size_t)nrows * sizeof(unsigned), st);
+  if (e) return e;
+  long long want = (n + CS_NT - 1) / CS_NT;
+  const int ctas = (int)(want < (long long)sms * 8 ? (want > 0 ? want : 1) : (long long)sms * 8);
+  k_row_hist<<<ctas, CS_NT, 0, st>>>(keys, n, nrows, count, err);
+  const int nb = (int)row_sort_block_sums(nrows);
+  k_scan_reduce<<<nb, CS_NT, 0, st>>>(count, nrows, block_sums);
+  k_scan_top<<<1, CS_NT, 0, st>>>(block_sums, nb);
+  k_scan_apply<<<nb, CS_NT, 0, st>>>(count, nrows, block_sums, row_start, cursor);
+  const long long chunks = (n + SCATTER_CHUNK - 1) / SCATTER_CHUNK;
+  const long long sblocks = (chunks + CS_NT / 32 - 1) / (CS_NT / 32);
+  k_row_scatter<<<(int)(sblocks < (long long)sms * 8 ? (sblocks > 0 ? sblocks : 1) : (long long)sms * 8), CS_NT, 0,
+                  st>>>(keys, n, nrows, cursor, perm, inv);
+  return cudaGetLastError();
+}
+
 }  // namespace pm
