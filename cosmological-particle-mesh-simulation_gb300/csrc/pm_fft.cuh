@@ -88,6 +88,36 @@ template <bool INV> struct DFT<8, INV> {
   }
 };
 
+// 16 = 4 x 4: j = 4 a + b, k = c + 4 d; twiddles w16^(b c) between the two radix-4 stages.
+template <bool INV> struct DFT<16, INV> {
+  static __device__ __forceinline__ void run(float2* v) {
+    const float c1 = 0.923879532511286756128f, s1 = 0.382683432365089771728f;  // cos, sin(pi/8)
+    const float h = 0.707106781186547524400844f;                              // sqrt(1/2)
+    // w16^m (forward: exp(-2 pi i m / 16)) for the products b c in {1, 2, 3, 4, 6, 9}
+    const float sg = INV ? 1.f : -1.f;
+    const float2 w1 = make_float2(c1, sg * s1), w2 = make_float2(h, sg * h), w3 = make_float2(s1, sg * c1);
+    const float2 w6 = make_float2(-h, sg * h), w9 = make_float2(-c1, -sg * s1);
+    float2 t[4][4];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      float2 x[4] = {v[b], v[4 + b], v[8 + b], v[12 + b]};
+      DFT<4, INV>::run(x);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) t[b][c] = x[c];
+    }
+    t[1][1] = cmul(t[1][1], w1); t[1][2] = cmul(t[1][2], w2); t[1][3] = cmul(t[1][3], w3);
+    t[2][1] = cmul(t[2][1], w2); t[2][2] = mul_mi<INV>(t[2][2]); t[2][3] = cmul(t[2][3], w6);
+    t[3][1] = cmul(t[3][1], w3); t[3][2] = cmul(t[3][2], w6); t[3][3] = cmul(t[3][3], w9);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      float2 y[4] = {t[0][c], t[1][c], t[2][c], t[3][c]};
+      DFT<4, INV>::run(y);
+#pragma unroll
+      for (int d = 0; d < 4; ++d) v[c + 4 * d] = y[d];
+    }
+  }
+};
+
 // ---------------------------------------------------------------------------------
 // Radix plans (product of radices == L)
 // ---------------------------------------------------------------------------------
@@ -187,6 +217,80 @@ __device__ __forceinline__ void fft_passes(float2* s, const float2* __restrict__
   }
 }
 
+// Lengths whose blocked transforms run on pairs of lines (the radix-3 plans hold too many
+// values per thread for it).
+__host__ __device__ constexpr bool blocked_pairs(int L) { return L % 3 != 0; }
+
+// The same pass over pairs of adjacent lines of the Blocked layout (BW even): the two lines
+// share their element addresses' 16-byte words, so every shared-memory access is a
+// float4 (half the instructions) and every twiddle serves both lines.
+template <int L, int R, int NS, int NL, int BW, int NT, bool INV, class EPI = NoEpi>
+__device__ __forceinline__ void stockham_pass_pairs(float2* s, const float2* __restrict__ tw, int tws,
+                                                    const EPI& epi = EPI()) {
+  static_assert(BW % 2 == 0 && NL % 2 == 0, "pairs of lines");
+  using LAY = Blocked<L, BW>;
+  constexpr int NB = L / R, NP = NL / 2;
+  constexpr int NTASK = NP * NB;
+  constexpr int TPT = (NTASK + NT - 1) / NT;
+  float4* s4 = reinterpret_cast<float4*>(s);
+  float2 a[TPT][R], b[TPT][R];
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    const int task = threadIdx.x + t * NT;
+    if ((NTASK % NT) == 0 || task < NTASK) {
+      const int line = 2 * (task % NP), j = task / NP;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const float4 q = s4[LAY::at(j + r * NB, line) >> 1];
+        a[t][r] = make_float2(q.x, q.y);
+        b[t][r] = make_float2(q.z, q.w);
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    const int task = threadIdx.x + t * NT;
+    if ((NTASK % NT) == 0 || task < NTASK) {
+      const int line = 2 * (task % NP), j = task / NP;
+      const int k = j % NS;
+      if (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          float2 w = __ldg(&tw[(r * k * (L / (NS * R))) * tws]);
+          if (INV) w.y = -w.y;
+          a[t][r] = cmul(a[t][r], w);
+          b[t][r] = cmul(b[t][r], w);
+        }
+      }
+      DFT<R, INV>::run(a[t]);
+      DFT<R, INV>::run(b[t]);
+      const int base = (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int e = base + r * NS;
+        const float2 x = epi(a[t][r], e, line), y = epi(b[t][r], e, line + 1);
+        s4[LAY::at(e, line) >> 1] = make_float4(x.x, x.y, y.x, y.y);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <int L, int P, int NS, int NL, int BW, int NT, bool INV, class EPI = NoEpi>
+__device__ __forceinline__ void fft_passes_pairs(float2* s, const float2* __restrict__ tw, int tws,
+                                                 const EPI& epi = EPI()) {
+  if constexpr (P < Plan<L>::np) {
+    constexpr int R = Plan<L>::r[P];
+    if constexpr (P + 1 == Plan<L>::np) {
+      stockham_pass_pairs<L, R, NS, NL, BW, NT, INV, EPI>(s, tw, tws, epi);
+    } else {
+      stockham_pass_pairs<L, R, NS, NL, BW, NT, INV>(s, tw, tws);
+      fft_passes_pairs<L, P + 1, NS * R, NL, BW, NT, INV, EPI>(s, tw, tws, epi);
+    }
+  }
+}
+
 // Unnormalised DFT of NL interleaved lines of length L held in shared memory.
 // Must be entered by all NT threads after a __syncthreads(); returns synchronised.
 template <int L, int NL, int LS, int NT, bool INV>
@@ -199,7 +303,10 @@ __device__ __forceinline__ void fft_lines(float2* s, const float2* __restrict__ 
 template <int L, int NL, int BW, int NT, bool INV, class EPI = NoEpi>
 __device__ __forceinline__ void fft_lines_blocked(float2* s, const float2* __restrict__ tw, int tws,
                                                   const EPI& epi = EPI()) {
-  fft_passes<L, 0, 1, NL, Blocked<L, BW>, NT, INV, EPI>(s, tw, tws, epi);
+  if constexpr (blocked_pairs(L))
+    fft_passes_pairs<L, 0, 1, NL, BW, NT, INV, EPI>(s, tw, tws, epi);
+  else
+    fft_passes<L, 0, 1, NL, Blocked<L, BW>, NT, INV, EPI>(s, tw, tws, epi);
 }
 
 }  // namespace pm

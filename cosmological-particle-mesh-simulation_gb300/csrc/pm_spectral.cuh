@@ -43,15 +43,24 @@ __host__ __device__ constexpr int cpitch(int n) { return (chalf(n) + 15) / 16 * 
 // Line passes that stream through a TMA ring: boxes of at most 256 rows tiling n.
 __host__ __device__ constexpr int line_box_rows(int n) { return n <= 256 ? n : (n % 256 == 0 ? 256 : n / 2); }
 __host__ __device__ constexpr bool tma_lines(int n) { return n >= 32 && line_box_rows(n) <= 256; }
-// Threads of a line-pass CTA: 1024 (64 registers each) where the transform fits in them;
-// the small odd sizes keep 512 (128 registers) to stay clear of spills.
-__host__ __device__ constexpr int line_nt(int n) { return n % 3 == 0 && n < 192 ? 512 : 1024; }
+// Threads of a line-pass CTA: 512 (pairs of lines, up to 128 registers); the radix-3 sizes
+// from 192 up, transformed line by line, run 1024.
+__host__ __device__ constexpr int line_nt(int n) { return n % 3 == 0 && n >= 192 ? 1024 : 512; }
 constexpr int XTMA_NT = 1024;  // x passes
 constexpr int TMA_STAGES = 3;
 __host__ __device__ constexpr size_t tma_stage_bytes(int n) {
   return (size_t)n * cline_width(n) * cline_bpc(n) * sizeof(float2);
 }
 __host__ __device__ constexpr size_t tma_smem_bytes(int n) { return TMA_STAGES * tma_stage_bytes(n) + 64; }
+
+// x passes with the row transform in registers (power-of-two n, 64 <= n <= 512): a row of
+// M = n/2 complex points is factored M = P x Q and held by T lanes of a warp
+__host__ __device__ constexpr bool xrow_ok(int n) { return n == 64 || n == 128 || n == 256 || n == 512; }
+__host__ __device__ constexpr int xrow_P(int n) { return n >= 256 ? 16 : 8; }
+__host__ __device__ constexpr int xrow_Q(int n) { return n / 2 / xrow_P(n); }
+__host__ __device__ constexpr int xrow_T(int n) { return xrow_Q(n) < xrow_P(n) ? xrow_Q(n) : xrow_P(n); }
+__host__ __device__ constexpr int xrow_rows_per_warp(int n) { return 32 / xrow_T(n); }
+constexpr int XR_NT = 256;
 
 // x passes fed by bulk copies into a double-buffered staging area (one simulation per launch)
 __host__ __device__ constexpr bool tma_rows(int n);
@@ -447,6 +456,109 @@ __global__ void __launch_bounds__(line_nt(N), 1) k_line_tma(const CUtensorMap* _
   if (threadIdx.x == 0) bulk_wait<0>();
 }
 
+// ---------------------------------------------------------------------------------
+// x passes, row transform in registers (xrow_ok sizes).  T lanes of a warp own one row of
+// M = P Q complex points, j = Q a + b, k = c + P d:
+//   pass 1  lane t, b = t + T i: P-point DFT over a of z[Q a + b], times w_M^(b c)
+//   (shared-memory exchange inside the row, synchronised by the warp alone)
+//   pass 2  lane t, c = t + T i: Q-point DFT over b -> Z[c + P d]
+// R2C: z[j] = x[2j] + i x[2j+1] read straight from the density rows, Z untangled into the
+// half spectrum.  C2R: the spectrum row is staged, tangled into pass 1, and z written as
+// pairs of reals.  Loads and stores of T lanes are consecutive (coalesced).  A work unit
+// is the 32 / T rows of one warp.
+// ---------------------------------------------------------------------------------
+template <int N, bool C2R>
+__global__ void __launch_bounds__(XR_NT) k_x_row(const Sim* __restrict__ sims, Work w) {
+  constexpr int M = N / 2, P = xrow_P(N), Q = xrow_Q(N), T = xrow_T(N), RPW = 32 / T;
+  constexpr int RB = Q * (P + 1);  // exchange buffer of a row (>= M + 1)
+  constexpr int NB1 = Q / T, NB2 = P / T;
+  static_assert(P * Q == M && Q % T == 0 && P % T == 0 && RB >= M + 1, "row plan");
+  __shared__ float2 sbuf[XR_NT / 32][RPW][RB];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int sub = lane / T, t = lane % T;
+  float2* rb = sbuf[wid][sub];
+  const long long nw = (long long)gridDim.x * (XR_NT / 32);
+  for (long long unit = (long long)blockIdx.x * (XR_NT / 32) + wid; unit < w.total; unit += nw) {
+    const int si = locate_sim(w, (int)unit);
+    const Sim& S = sims[si];
+    const long long row = ((long long)unit - __ldg(&w.prefix[si])) * RPW + sub;
+    const float2* __restrict__ tw = S.tw;
+    float2 v[NB1][P];
+    if (!C2R) {
+      const float2* __restrict__ src = reinterpret_cast<const float2*>(S.rho) + row * M;
+#pragma unroll
+      for (int i = 0; i < NB1; ++i)
+#pragma unroll
+        for (int a = 0; a < P; ++a) v[i][a] = __ldg(&src[Q * a + t + T * i]);
+    } else {
+      const float2* __restrict__ src = S.spec + row * S.pitch;
+      __syncwarp();
+      for (int k = t; k <= M; k += T) rb[k] = __ldg(&src[k]);
+      __syncwarp();
+      // tangle: Z[j] = (X[j] + X*[M-j]) + i W^-j (X[j] - X*[M-j])
+#pragma unroll
+      for (int i = 0; i < NB1; ++i)
+#pragma unroll
+        for (int a = 0; a < P; ++a) {
+          const int j = Q * a + t + T * i;
+          const float2 xk = rb[j], xm = rb[M - j];
+          const float2 ap = cadd(xk, conjf2(xm)), bm = csub(xk, conjf2(xm));
+          const float2 tt = cmul(conjf2(__ldg(&tw[j])), bm);
+          v[i][a] = make_float2(ap.x - tt.y, ap.y + tt.x);
+        }
+    }
+    // pass 1
+#pragma unroll
+    for (int i = 0; i < NB1; ++i) {
+      const int b = t + T * i;
+      DFT<P, C2R>::run(v[i]);
+#pragma unroll
+      for (int c = 1; c < P; ++c) {
+        float2 wv = __ldg(&tw[((b * c) % M) * 2]);
+        if (C2R) wv.y = -wv.y;
+        v[i][c] = cmul(v[i][c], wv);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < NB1; ++i)
+#pragma unroll
+      for (int c = 0; c < P; ++c) rb[(t + T * i) * (P + 1) + c] = v[i][c];
+    __syncwarp();
+    // pass 2
+    float2 o[NB2][Q];
+#pragma unroll
+    for (int i = 0; i < NB2; ++i) {
+#pragma unroll
+      for (int b = 0; b < Q; ++b) o[i][b] = rb[b * (P + 1) + t + T * i];
+      DFT<Q, C2R>::run(o[i]);
+    }
+    if (!C2R) {
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < NB2; ++i)
+#pragma unroll
+        for (int d = 0; d < Q; ++d) rb[t + T * i + P * d] = o[i][d];
+      __syncwarp();
+      // untangle: X[k] = E[k] + W^k O[k], k = 0..M
+      float2* __restrict__ dst = S.spec + row * S.pitch;
+      for (int k = t; k <= M; k += T) {
+        const float2 zk = rb[k == M ? 0 : k];
+        const float2 zc = conjf2(rb[k == 0 ? 0 : M - k]);
+        const float2 e = cscale(cadd(zk, zc), 0.5f);
+        const float2 od = cscale(mul_mi<false>(csub(zk, zc)), 0.5f);
+        dst[k] = cadd(e, cmul(__ldg(&tw[k]), od));
+      }
+    } else {
+      float2* __restrict__ dst = reinterpret_cast<float2*>(S.phi) + row * M;
+#pragma unroll
+      for (int i = 0; i < NB2; ++i)
+#pragma unroll
+        for (int d = 0; d < Q; ++d) dst[t + T * i + P * d] = o[i][d];
+    }
+  }
+}
+
 // Tensor map of a half spectrum seen as float32 [z][y][2*pitch], box {2 BW, BOX, 1} for the
 // y pass and {2 BW, 1, BOX} for the z pass.
 inline bool encode_spectrum_map(CUtensorMap* tm, const void* spec, int n, bool zaxis) {
@@ -718,6 +830,15 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
   }
   if (kind == SPEC_PREPARE) return cudaSuccess;
   const int grid = w.total < device_sms() ? w.total : device_sms();
+  if constexpr (xrow_ok(N)) {
+    if (kind == SPEC_X_R2C || kind == SPEC_X_C2R) {
+      const int per = XR_NT / 32, want = (w.total + per - 1) / per, cap = device_sms() * 8;
+      const int g = want < cap ? want : cap;
+      if (kind == SPEC_X_R2C) k_x_row<N, false><<<g, XR_NT, 0, st>>>(sims, w);
+      else k_x_row<N, true><<<g, XR_NT, 0, st>>>(sims, w);
+      return cudaGetLastError();
+    }
+  }
   if constexpr (tma_rows(N)) {
     if (kind == SPEC_X_R2C || kind == SPEC_X_C2R) {
       if (kind == SPEC_X_R2C) k_x_tma<N, false><<<grid, XTMA_NT, xtma_smem_bytes(N), st>>>(sims, w, err);

@@ -42,6 +42,7 @@ bool spectral_supported(int n) {
 }
 
 long long spectral_units(SpecKind kind, int n) {
+  if ((kind == SPEC_X_R2C || kind == SPEC_X_C2R) && xrow_ok(n)) return (long long)n * n / xrow_rows_per_warp(n);
   if (kind == SPEC_X_R2C || kind == SPEC_X_C2R) {
     const long long rows = (long long)n * n, nr = cx_rows(n);
     return (rows + nr - 1) / nr;
