@@ -369,7 +369,7 @@ int pm_step(pm_ctx* c, float* positions, float* velocities, long long np, double
     PM_CK(launch_row_start(skeys, np, k.sim.xbits, (unsigned)nrows, c->row_start.as<unsigned>(), st), "rows");
     PM_CK(deposit_r2c_dispatch(c->n, c->d_sim.as<Sim>(), work(c, k, PH_DEP), k.parts, perm,
                                c->row_start.as<unsigned>(), POS_ABS, c->d_err.as<int>(),
-                               grid_for(k.prefix[PH_DEP][1], c->sms, 4), st),
+                               grid_for(k.prefix[PH_DEP][1], c->sms, deposit_r2c_ctas_per_sm(c->n)), st),
           "fused deposit");
     if (int r = spectral(c, k, false, st, true)) return r;
     return kick(c, k, perm, st);

@@ -50,7 +50,7 @@ struct Plan {
   int max_n = 0;
 };
 
-const int kStateArrays = 7;
+const int kStateArrays = 11;  // x y z vx vy vz id, cell record: cell fx fy fz
 
 }  // namespace
 
@@ -62,7 +62,7 @@ struct pm_batch {
   std::map<int, std::unique_ptr<Tables>> tables;
   std::map<long long, std::unique_ptr<Lattice>> lattices;
   int next_id = 1;
-  // particle state, two copies; arrays x y z vx vy vz id
+  // particle state, two copies; arrays x y z vx vy vz id and the cell record cell fx fy fz
   DBuf st[2][kStateArrays];
   long long pcap = 0;
   int cur = 0;
@@ -104,6 +104,10 @@ Parts state(pm_batch* b, int which) {
   p.vy = b->st[which][4].as<float>();
   p.vz = b->st[which][5].as<float>();
   p.id = b->st[which][6].as<unsigned>();
+  p.cell = b->st[which][7].as<unsigned>();
+  p.fx = b->st[which][8].as<float>();
+  p.fy = b->st[which][9].as<float>();
+  p.fz = b->st[which][10].as<float>();
   return p;
 }
 
@@ -340,7 +344,8 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
     if (!P.fused[g]) continue;
     const int tot = P.fdep_total[g];
     PB_CK(deposit_r2c_dispatch(P.sizes[g], ds, work_of(b, PH_FIXED + 3 * (int)g + 2, tot), in, perm,
-                               b->row_start.as<unsigned>(), POS_DISP, err, grid_for(tot, b->sms, 4), st),
+                               b->row_start.as<unsigned>(), POS_DISP, err,
+                               grid_for(tot, b->sms, deposit_r2c_ctas_per_sm(P.sizes[g])), st),
           "fused deposit");
   }
   PB_CK(mark(1 + PP_DEPOSIT), "event");

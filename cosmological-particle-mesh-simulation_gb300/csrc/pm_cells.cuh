@@ -81,9 +81,34 @@ __device__ __forceinline__ Cell cell_disp(const Sim& S, unsigned id, float dx, f
   return c;
 }
 
+constexpr unsigned CELL_BAD = 0xffffffffu;
+
+__device__ __forceinline__ void store_cell_record(const Parts& p, long long i, const Cell& c) {
+  p.cell[i] = c.ok ? ((unsigned)c.x | ((unsigned)c.y << 10) | ((unsigned)c.z << 20)) : CELL_BAD;
+  p.fx[i] = c.fx;
+  p.fy[i] = c.fy;
+  p.fz[i] = c.fz;
+}
+
+__device__ __forceinline__ Cell load_cell_record(const Parts& p, long long i) {
+  Cell c;
+  const unsigned k = p.cell[i];
+  c.ok = k != CELL_BAD;
+  c.x = (int)(k & 1023u);
+  c.y = (int)((k >> 10) & 1023u);
+  c.z = (int)((k >> 20) & 1023u);
+  c.fx = p.fx[i];
+  c.fy = p.fy[i];
+  c.fz = p.fz[i];
+  return c;
+}
+
+// The base cell of a particle: from its absolute position, its cell record, or its
+// displacement (POS_DISP without records).
 template <int MODE>
 __device__ __forceinline__ Cell particle_cell(const Sim& S, const Parts& p, long long slot) {
   if (MODE == POS_ABS) return cell_abs(p.x[slot], p.y[slot], p.z[slot], S.n);
+  if (p.cell) return load_cell_record(p, slot);
   return cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
 }
 

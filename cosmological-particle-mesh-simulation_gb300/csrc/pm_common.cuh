@@ -71,6 +71,11 @@ struct Parts {
   float* x; float* y; float* z;       // positions (POS_ABS) or displacements (POS_DISP)
   float* vx; float* vy; float* vz;
   unsigned* id;                        // Lagrangian particle index (POS_DISP)
+  // cell record (POS_DISP, optional): base cell packed x | y << 10 | z << 20 (CELL_BAD if
+  // not finite) and the in-cell offsets, exactly as computed from the displacement; written
+  // with the state by the kick so that the deposit reads the cell instead of recomputing it
+  unsigned* cell;
+  float* fx; float* fy; float* fz;
 };
 
 __device__ __forceinline__ int locate_sim(const Work& w, int unit) {
@@ -115,6 +120,7 @@ template <int N>
 cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned* perm, const unsigned* row_start,
                                int mode, int* err, int ctas, cudaStream_t st);
 bool deposit_r2c_supported(int n);
+int deposit_r2c_ctas_per_sm(int n);  // resident CTAs per SM of the fused deposit
 cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const unsigned* perm,
                                  const unsigned* row_start, int mode, int* err, int ctas, cudaStream_t st);
 

@@ -12,6 +12,7 @@
 namespace pm {
 
 constexpr int DEP_NT = 512;
+constexpr int DEP_ROW_NT = 256;  // fused deposit with the register row transform
 
 __device__ __forceinline__ void acc_add(unsigned* lo, unsigned* hi, int i, unsigned q) {
   const unsigned old = atomicAdd(&lo[i], q);
@@ -23,15 +24,16 @@ __device__ __forceinline__ float fixed_to_float(unsigned l, unsigned h, float sc
 }
 
 // Adds the 8 weights of a particle with base cell (cx, ly, lz) (ly, lz relative to the
-// tile, in [-1, TY-1] x [-1, TZ-1]) to the tile accumulators.
-__device__ __forceinline__ void deposit_particle(unsigned* lo, unsigned* hi, int n, int cx, int ly, int lz,
+// tile, in [-1, TY-1] x [-1, TZ-1]) to the tile accumulators; tile row r of lo / hi starts
+// at word r * rs.
+__device__ __forceinline__ void deposit_particle(unsigned* lo, unsigned* hi, int n, int rs, int cx, int ly, int lz,
                                                  const float (&wt)[8]) {
   const int x1 = cx + 1 == n ? 0 : cx + 1;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     const int ty2 = ly + corner_y(k), tz2 = lz + corner_z(k);
     if (ty2 >= 0 && ty2 < TY && tz2 >= 0 && tz2 < TZ)
-      acc_add(lo, hi, (tz2 * TY + ty2) * n + (corner_x(k) ? x1 : cx),
+      acc_add(lo, hi, (tz2 * TY + ty2) * rs + (corner_x(k) ? x1 : cx),
               __float2uint_rn(wt[k] * (float)(1u << PM_FIX_BITS)));
   }
 }
@@ -60,15 +62,16 @@ __device__ __forceinline__ bool source_cell(const Sim& S, const Parts& p, const 
   return ok;
 }
 
-// Accumulate the tile at (y0, z0) of simulation S into lo/hi (TZ * TY * n cells each).
+// Accumulate the tile at (y0, z0) of simulation S into lo/hi (TZ * TY rows of n cells,
+// row r at word r * rs of each; lo and hi together are 2 * TZ * TY * n contiguous words).
 // Entered and left by all NT threads, synchronised.
 template <int MODE, int NT>
 __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
                                              const unsigned* __restrict__ row_start, int* err, int y0, int z0,
-                                             unsigned* lo, unsigned* hi, unsigned* s_begin, unsigned* s_off) {
+                                             unsigned* lo, unsigned* hi, int rs, unsigned* s_begin, unsigned* s_off) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n = S.n;
-  const int ncell = TZ * TY * n;  // lo and hi are contiguous: zero 2 * ncell words
+  const int ncell = TZ * TY * n;  // zero 2 * ncell words
   uint4* z4 = reinterpret_cast<uint4*>(lo);
   for (int i = threadIdx.x; i < ncell / 2; i += NT) z4[i] = make_uint4(0u, 0u, 0u, 0u);
   if (warp == 0) {
@@ -106,12 +109,12 @@ __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const
     if (ok0) {
       float wt[8];
       cic_weights(c0, wt);
-      deposit_particle(lo, hi, n, c0.x, ly0, lz0, wt);
+      deposit_particle(lo, hi, n, rs, c0.x, ly0, lz0, wt);
     }
     if (ok1) {
       float wt[8];
       cic_weights(c1, wt);
-      deposit_particle(lo, hi, n, c1.x, ly1, lz1, wt);
+      deposit_particle(lo, hi, n, rs, c1.x, ly1, lz1, wt);
     }
   }
   __syncthreads();

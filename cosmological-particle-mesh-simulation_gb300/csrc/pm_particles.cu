@@ -33,7 +33,10 @@ __global__ void __launch_bounds__(KEY_NT) k_keys(const Sim* __restrict__ sims, W
     const long long i = (long long)(unit - __ldg(&w.prefix[si])) * KEY_NT + threadIdx.x;
     if (i >= S.np) continue;
     const long long slot = S.part_off + i;
-    Cell c = particle_cell<MODE>(S, p, slot);
+    // from the state itself (the cell records, if any, are written here)
+    Cell c = MODE == POS_ABS ? cell_abs(p.x[slot], p.y[slot], p.z[slot], S.n)
+                             : cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
+    if (MODE == POS_DISP && p.cell) store_cell_record(p, slot, c);
     if (!c.ok) { set_error(err, ERR_CELL_RANGE); c.x = c.y = c.z = 0; }
     keys[slot] = cell_key(S, c);
     if (vals) vals[slot] = (unsigned)slot;
@@ -75,7 +78,7 @@ __global__ void __launch_bounds__(DEP_NT, 3) k_deposit(const Sim* __restrict__ s
     const int y0 = (local % ntile_y) * TY, z0 = (local / ntile_y) * TZ;
     unsigned* lo = reinterpret_cast<unsigned*>(acc_raw);
     unsigned* hi = lo + TZ * TY * n;
-    deposit_tile<MODE, DEP_NT>(S, p, perm, row_start, err, y0, z0, lo, hi, s_begin, s_off);
+    deposit_tile<MODE, DEP_NT>(S, p, perm, row_start, err, y0, z0, lo, hi, S.n, s_begin, s_off);
     const float ms = S.mass_scale;
     for (int row = warp; row < TZ * TY; row += DEP_NT / 32) {
       const uint4* l4 = reinterpret_cast<const uint4*>(lo + row * n);
@@ -213,6 +216,7 @@ __device__ __forceinline__ void kick_store(const Sim& S, const Parts& out, long 
     out.id[sp] = id;
     if (keys_next) {
       Cell cn = cell_disp(S, id, nx, ny, nz);
+      if (out.cell) store_cell_record(out, sp, cn);
       if (!cn.ok) { set_error(err, ERR_CELL_RANGE); cn.x = cn.y = cn.z = 0; }
       keys_next[sp] = cell_key(S, cn);
     }

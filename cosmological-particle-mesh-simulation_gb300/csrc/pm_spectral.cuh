@@ -467,6 +467,60 @@ __global__ void __launch_bounds__(line_nt(N), 1) k_line_tma(const CUtensorMap* _
 // pairs of reals.  Loads and stores of T lanes are consecutive (coalesced).  A work unit
 // is the 32 / T rows of one warp.
 // ---------------------------------------------------------------------------------
+// Pass 1, the in-row exchange and pass 2 of a row transform; v holds z[Q a + t + T i] on
+// entry, o holds Z[t + T i + P d] on exit.  rb: the row's exchange buffer (Q (P + 1)).
+template <int N, bool INV>
+__device__ __forceinline__ void xrow_transform(float2 (&v)[xrow_Q(N) / xrow_T(N)][xrow_P(N)],
+                                               float2 (&o)[xrow_P(N) / xrow_T(N)][xrow_Q(N)], float2* rb, int t,
+                                               const float2* __restrict__ tw) {
+  constexpr int M = N / 2, P = xrow_P(N), Q = xrow_Q(N), T = xrow_T(N);
+  constexpr int NB1 = Q / T, NB2 = P / T;
+#pragma unroll
+  for (int i = 0; i < NB1; ++i) {
+    const int b = t + T * i;
+    DFT<P, INV>::run(v[i]);
+#pragma unroll
+    for (int c = 1; c < P; ++c) {
+      float2 wv = __ldg(&tw[((b * c) % M) * 2]);
+      if (INV) wv.y = -wv.y;
+      v[i][c] = cmul(v[i][c], wv);
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < NB1; ++i)
+#pragma unroll
+    for (int c = 0; c < P; ++c) rb[(t + T * i) * (P + 1) + c] = v[i][c];
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < NB2; ++i) {
+#pragma unroll
+    for (int b = 0; b < Q; ++b) o[i][b] = rb[b * (P + 1) + t + T * i];
+    DFT<Q, INV>::run(o[i]);
+  }
+}
+
+// R2C end of a row: Z (in o) is untangled into the half-spectrum row dst[0..M].
+template <int N>
+__device__ __forceinline__ void xrow_untangle_store(const float2 (&o)[xrow_P(N) / xrow_T(N)][xrow_Q(N)], float2* rb,
+                                                    int t, const float2* __restrict__ tw, float2* __restrict__ dst) {
+  constexpr int M = N / 2, P = xrow_P(N), Q = xrow_Q(N), T = xrow_T(N), NB2 = P / T;
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < NB2; ++i)
+#pragma unroll
+    for (int d = 0; d < Q; ++d) rb[t + T * i + P * d] = o[i][d];
+  __syncwarp();
+  // X[k] = E[k] + W^k O[k], k = 0..M
+  for (int k = t; k <= M; k += T) {
+    const float2 zk = rb[k == M ? 0 : k];
+    const float2 zc = conjf2(rb[k == 0 ? 0 : M - k]);
+    const float2 e = cscale(cadd(zk, zc), 0.5f);
+    const float2 od = cscale(mul_mi<false>(csub(zk, zc)), 0.5f);
+    dst[k] = cadd(e, cmul(__ldg(&tw[k]), od));
+  }
+}
+
 template <int N, bool C2R>
 __global__ void __launch_bounds__(XR_NT) k_x_row(const Sim* __restrict__ sims, Work w) {
   constexpr int M = N / 2, P = xrow_P(N), Q = xrow_Q(N), T = xrow_T(N), RPW = 32 / T;
@@ -484,12 +538,15 @@ __global__ void __launch_bounds__(XR_NT) k_x_row(const Sim* __restrict__ sims, W
     const long long row = ((long long)unit - __ldg(&w.prefix[si])) * RPW + sub;
     const float2* __restrict__ tw = S.tw;
     float2 v[NB1][P];
+    float2 o[NB2][Q];
     if (!C2R) {
       const float2* __restrict__ src = reinterpret_cast<const float2*>(S.rho) + row * M;
 #pragma unroll
       for (int i = 0; i < NB1; ++i)
 #pragma unroll
         for (int a = 0; a < P; ++a) v[i][a] = __ldg(&src[Q * a + t + T * i]);
+      xrow_transform<N, false>(v, o, rb, t, tw);
+      xrow_untangle_store<N>(o, rb, t, tw, S.spec + row * S.pitch);
     } else {
       const float2* __restrict__ src = S.spec + row * S.pitch;
       __syncwarp();
@@ -506,50 +563,7 @@ __global__ void __launch_bounds__(XR_NT) k_x_row(const Sim* __restrict__ sims, W
           const float2 tt = cmul(conjf2(__ldg(&tw[j])), bm);
           v[i][a] = make_float2(ap.x - tt.y, ap.y + tt.x);
         }
-    }
-    // pass 1
-#pragma unroll
-    for (int i = 0; i < NB1; ++i) {
-      const int b = t + T * i;
-      DFT<P, C2R>::run(v[i]);
-#pragma unroll
-      for (int c = 1; c < P; ++c) {
-        float2 wv = __ldg(&tw[((b * c) % M) * 2]);
-        if (C2R) wv.y = -wv.y;
-        v[i][c] = cmul(v[i][c], wv);
-      }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int i = 0; i < NB1; ++i)
-#pragma unroll
-      for (int c = 0; c < P; ++c) rb[(t + T * i) * (P + 1) + c] = v[i][c];
-    __syncwarp();
-    // pass 2
-    float2 o[NB2][Q];
-#pragma unroll
-    for (int i = 0; i < NB2; ++i) {
-#pragma unroll
-      for (int b = 0; b < Q; ++b) o[i][b] = rb[b * (P + 1) + t + T * i];
-      DFT<Q, C2R>::run(o[i]);
-    }
-    if (!C2R) {
-      __syncwarp();
-#pragma unroll
-      for (int i = 0; i < NB2; ++i)
-#pragma unroll
-        for (int d = 0; d < Q; ++d) rb[t + T * i + P * d] = o[i][d];
-      __syncwarp();
-      // untangle: X[k] = E[k] + W^k O[k], k = 0..M
-      float2* __restrict__ dst = S.spec + row * S.pitch;
-      for (int k = t; k <= M; k += T) {
-        const float2 zk = rb[k == M ? 0 : k];
-        const float2 zc = conjf2(rb[k == 0 ? 0 : M - k]);
-        const float2 e = cscale(cadd(zk, zc), 0.5f);
-        const float2 od = cscale(mul_mi<false>(csub(zk, zc)), 0.5f);
-        dst[k] = cadd(e, cmul(__ldg(&tw[k]), od));
-      }
-    } else {
+      xrow_transform<N, true>(v, o, rb, t, tw);
       float2* __restrict__ dst = reinterpret_cast<float2*>(S.phi) + row * M;
 #pragma unroll
       for (int i = 0; i < NB2; ++i)
@@ -705,29 +719,35 @@ __global__ void __launch_bounds__(XTMA_NT, 1) k_x_tma(const Sim* __restrict__ si
 
 // ---------------------------------------------------------------------------------
 // fused deposit + x R2C: one CTA per deposit tile.  The tile's TZ x TY rows are deposited
-// into shared memory (pm_deposit.cuh), converted to float, transposed into the padded
-// line-interleaved FFT buffer (reusing the accumulator space) and transformed along x;
-// the half-spectrum rows are written directly, so the density grid never goes to HBM.
+// into shared memory (pm_deposit.cuh), converted to float and transformed along x -- by
+// the register row transform (T lanes per row) where the size has one, else transposed
+// into a padded line-interleaved buffer (reusing the accumulator space) -- and the
+// half-spectrum rows are written directly, so the density grid never goes to HBM.
 // ---------------------------------------------------------------------------------
-__host__ __device__ constexpr size_t deposit_r2c_smem_bytes(int n) {
-  return (size_t)2 * TZ * TY * n * sizeof(unsigned);  // >= (n/2) * (TZ*TY + 1) * sizeof(float2)
-}
+// accumulators: 2 words per cell, >= (n/2) * (TZ*TY + 1) * sizeof(float2) for the
+// shared-memory transform; with the register row transform each row's low and high words
+// are adjacent (row r at word 2 r n) and the row's exchange buffer overlays them
+__host__ __device__ constexpr size_t deposit_r2c_smem_bytes(int n) { return (size_t)2 * TZ * TY * n * sizeof(unsigned); }
+__host__ __device__ constexpr int deposit_r2c_nt(int n) { return xrow_ok(n) ? DEP_ROW_NT : DEP_NT; }
 // sizes whose tile (TZ * TY rows of n cells) divides evenly over the block
-__host__ __device__ constexpr bool deposit_r2c_ok(int n) { return (TZ * TY * n) % DEP_NT == 0; }
+__host__ __device__ constexpr bool deposit_r2c_ok(int n) { return (TZ * TY * n) % deposit_r2c_nt(n) == 0; }
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(DEP_NT, 2) k_deposit_r2c(const Sim* __restrict__ sims, Work w, Parts p,
-                                                           const unsigned* __restrict__ perm,
-                                                           const unsigned* __restrict__ row_start, int* err) {
+__global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
+    k_deposit_r2c(const Sim* __restrict__ sims, Work w, Parts p, const unsigned* __restrict__ perm,
+                  const unsigned* __restrict__ row_start, int* err) {
+  constexpr int NT = deposit_r2c_nt(N);
   constexpr int M = N / 2, NL = TZ * TY, LS = NL + 1;
-  constexpr int PER = NL * N / DEP_NT;
-  static_assert(NL * N % DEP_NT == 0, "tile cells must divide by the block size");
+  constexpr int PER = NL * N / NT;
+  static_assert(NL * N % NT == 0, "tile cells must divide by the block size");
   static_assert((size_t)M * LS * sizeof(float2) <= deposit_r2c_smem_bytes(N), "FFT buffer must fit");
   extern __shared__ uint4 acc_raw[];
   __shared__ unsigned s_begin[NSRC];
   __shared__ unsigned s_off[NSRC + 1];
   unsigned* lo = reinterpret_cast<unsigned*>(acc_raw);
-  unsigned* hi = lo + NL * N;
+  // row r: lo at r * RS, hi at r * RS + HO
+  constexpr int RS = xrow_ok(N) ? 2 * N : N, HO = xrow_ok(N) ? N : NL * N;
+  unsigned* hi = lo + HO;
   float2* F = reinterpret_cast<float2*>(acc_raw);
   float* Ff = reinterpret_cast<float*>(acc_raw);
   for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
@@ -735,26 +755,55 @@ __global__ void __launch_bounds__(DEP_NT, 2) k_deposit_r2c(const Sim* __restrict
     const Sim& S = sims[si];
     const int local = unit - __ldg(&w.prefix[si]);
     const int y0 = (local % (N / TY)) * TY, z0 = (local / (N / TY)) * TZ;
-    deposit_tile<MODE, DEP_NT>(S, p, perm, row_start, err, y0, z0, lo, hi, s_begin, s_off);
+    deposit_tile<MODE, NT>(S, p, perm, row_start, err, y0, z0, lo, hi, RS, s_begin, s_off);
     const float ms = S.mass_scale;
+    if constexpr (xrow_ok(N)) {
+      // the tile's NL rows: T lanes per row, rows r = warp * RPW + sub; the row's exchange
+      // buffer overlays its own accumulator words once they are read
+      constexpr int P = xrow_P(N), Q = xrow_Q(N), T = xrow_T(N), RPW = 32 / T;
+      constexpr int NB1 = Q / T, NB2 = P / T;
+      static_assert(Q * (P + 1) * sizeof(float2) <= 2 * N * sizeof(unsigned), "exchange buffer in the row");
+      const int lane = threadIdx.x & 31, sub = lane / T, t = lane % T;
+      const int r = (threadIdx.x >> 5) * RPW + sub;
+      float2* rb = reinterpret_cast<float2*>(lo + r * RS);
+      if ((threadIdx.x >> 5) * RPW < NL) {  // warp-uniform
+        float2 v2[NB1][P];
+        float2 o2[NB2][Q];
+        const uint2* l2 = reinterpret_cast<const uint2*>(lo + r * RS);
+        const uint2* h2 = reinterpret_cast<const uint2*>(lo + r * RS + HO);
+#pragma unroll
+        for (int i = 0; i < NB1; ++i)
+#pragma unroll
+          for (int a = 0; a < P; ++a) {
+            const int j = Q * a + t + T * i;  // z[j] = x[2j] + i x[2j+1]
+            const uint2 ll = l2[j], hh = h2[j];
+            v2[i][a] = make_float2(fixed_to_float(ll.x, hh.x, ms), fixed_to_float(ll.y, hh.y, ms));
+          }
+        xrow_transform<N, false>(v2, o2, rb, t, S.tw);
+        const long long row = (long long)(z0 + r / TY) * N + (y0 + r % TY);
+        xrow_untangle_store<N>(o2, rb, t, S.tw, S.spec + row * S.pitch);
+      }
+      __syncthreads();
+      continue;
+    }
     float v[PER];
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-      const int i = threadIdx.x + k * DEP_NT;
+      const int i = threadIdx.x + k * NT;
       v[k] = fixed_to_float(lo[i], hi[i], ms);
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-      const int i = threadIdx.x + k * DEP_NT;
+      const int i = threadIdx.x + k * NT;
       const int r = i / N, x = i % N;
       Ff[((x >> 1) * LS + r) * 2 + (x & 1)] = v[k];  // z[j] = x[2j] + i x[2j+1] of row r
     }
     __syncthreads();
-    fft_lines<M, NL, LS, DEP_NT, false>(F, S.tw, 2);
+    fft_lines<M, NL, LS, NT, false>(F, S.tw, 2);
     float2* __restrict__ dst = S.spec;
     const int P = S.pitch;
-    for (int u = threadIdx.x; u < NL * (M + 1); u += DEP_NT) {
+    for (int u = threadIdx.x; u < NL * (M + 1); u += NT) {
       const int r = u / (M + 1), k = u % (M + 1);
       const long long row = (long long)(z0 + r / TY) * N + (y0 + r % TY);
       const float2 zk = F[(k == M ? 0 : k) * LS + r];
@@ -784,8 +833,9 @@ cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned*
     init = true;
   }
   if (ctas <= 0) return cudaSuccess;  // attribute setup only
-  if (mode == POS_ABS) k_deposit_r2c<N, POS_ABS><<<ctas, DEP_NT, sm, st>>>(sims, w, p, perm, row_start, err);
-  else k_deposit_r2c<N, POS_DISP><<<ctas, DEP_NT, sm, st>>>(sims, w, p, perm, row_start, err);
+  constexpr int NT = deposit_r2c_nt(N);
+  if (mode == POS_ABS) k_deposit_r2c<N, POS_ABS><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err);
+  else k_deposit_r2c<N, POS_DISP><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err);
   return cudaGetLastError();
   }
 }

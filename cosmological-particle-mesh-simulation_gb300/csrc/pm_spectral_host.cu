@@ -30,7 +30,9 @@ bool spectral_encode_maps(int n, const void* spec, CUtensorMap out[2]) {
   return encode_spectrum_map(&out[0], spec, n, false) && encode_spectrum_map(&out[1], spec, n, true);
 }
 
-bool deposit_r2c_supported(int n) { return (TZ * TY * n) % DEP_NT == 0; }
+bool deposit_r2c_supported(int n) { return spectral_supported(n) && deposit_r2c_ok(n); }
+
+int deposit_r2c_ctas_per_sm(int n) { return xrow_ok(n) ? 3 : 2; }
 
 bool spectral_supported(int n) {
   switch (n) {
