@@ -15,6 +15,10 @@ struct pm_ctx {
   DBuf row_start, spec, phi, rho;     // scratch grids
   DBuf hpos, hvel;                    // device copies for pm_step_host
   DBuf pk_partial, pk_out;            // power spectrum scratch
+  DBuf row_count, row_cursor, scan_sums;  // counting sort of row keys
+  DBuf spos, svel;                        // the state in row order (drop-in step)
+  cudaStream_t side = nullptr;            // velocity copy of pm_step_host
+  cudaEvent_t ev_start = nullptr, ev_vel = nullptr;
   std::vector<double> pk_host;
   std::string err;
 };
@@ -127,11 +131,31 @@ int sort_particles(pm_ctx* c, Call& k, cudaStream_t st, unsigned** perm, unsigne
   return PM_OK;
 }
 
-int deposit(pm_ctx* c, Call& k, unsigned* perm, unsigned* skeys, cudaStream_t st) {
-  const long long nrows = (long long)c->n * c->n;
-  PM_CK(c->row_start.ensure((nrows + 1) * sizeof(unsigned)), "alloc rows");
-  PM_CK(launch_row_start(skeys, k.sim.np, k.sim.xbits, (unsigned)nrows, c->row_start.as<unsigned>(), st),
-        "rows");
+// keys (x-row numbers: k.sim.xbits must be 0) -> counting sort: row starts in c->row_start
+// and the permutation to row order.  The deposit and the kick need the particles grouped
+// by row only; their results do not depend on the order inside a row.
+int group_particles(pm_ctx* c, Call& k, cudaStream_t st, unsigned** perm, unsigned* inv = nullptr,
+                    float* pos_copy = nullptr) {
+  const long long np = k.sim.np;
+  const unsigned nrows = (unsigned)((long long)c->n * c->n);
+  PM_CK(c->sort.ensure(np), "alloc sort");
+  PM_CK(c->row_start.ensure(((size_t)nrows + 1) * sizeof(unsigned)), "alloc rows");
+  PM_CK(c->row_count.ensure((size_t)nrows * sizeof(unsigned)), "alloc rows");
+  PM_CK(c->row_cursor.ensure((size_t)nrows * sizeof(unsigned)), "alloc rows");
+  PM_CK(c->scan_sums.ensure(row_sort_block_sums(nrows) * sizeof(unsigned)), "alloc rows");
+  PM_CK(launch_keys_abs(c->d_sim.as<Sim>(), work(c, k, PH_KEYS), k.parts, c->sort.keys.as<unsigned>(), nullptr,
+                        c->d_err.as<int>(), grid_for(k.prefix[PH_KEYS][1], c->sms, 16), st,
+                        pos_copy ? abs_parts(pos_copy, nullptr, np) : Parts{}),
+        "keys");
+  *perm = c->sort.vals.as<unsigned>();
+  PM_CK(row_counting_sort(c->sort.keys.as<unsigned>(), np, nrows, c->row_count.as<unsigned>(),
+                          c->row_start.as<unsigned>(), c->row_cursor.as<unsigned>(), c->scan_sums.as<unsigned>(),
+                          *perm, c->d_err.as<int>(), c->sms, st, inv),
+        "sort");
+  return PM_OK;
+}
+
+int deposit(pm_ctx* c, Call& k, unsigned* perm, cudaStream_t st) {
   PM_CK(launch_deposit(c->d_sim.as<Sim>(), work(c, k, PH_DEP), k.parts, perm, c->row_start.as<unsigned>(),
                        POS_ABS, c->d_err.as<int>(), grid_for(k.prefix[PH_DEP][1], c->sms, 8),
                        deposit_smem_bytes(c->n, TILE_Y, TILE_Z), st),
@@ -243,6 +267,14 @@ void pm_ctx_destroy(pm_ctx* c) {
   c->hvel.release();
   c->pk_partial.release();
   c->pk_out.release();
+  c->row_count.release();
+  c->spos.release();
+  c->svel.release();
+  if (c->side) cudaStreamDestroy(c->side);
+  if (c->ev_start) cudaEventDestroy(c->ev_start);
+  if (c->ev_vel) cudaEventDestroy(c->ev_vel);
+  c->row_cursor.release();
+  c->scan_sums.release();
   delete c;
 }
 
@@ -266,14 +298,19 @@ int pm_density(pm_ctx* c, const float* positions, long long np, double mass, flo
   cudaStream_t st = (cudaStream_t)stream;
   Call k;
   k.sim = base_sim(c, np);
+  k.sim.xbits = 0;  // row keys
   k.sim.rho = rho;
   k.sim.mass_scale = (float)(mass / (double)(1u << PM_FIX_BITS));
   set_prefix(k, np, c->n);
   k.parts = abs_parts(const_cast<float*>(positions), nullptr, np);
   if (int r = upload(c, k, st)) return r;
-  unsigned *perm = nullptr, *skeys = nullptr;
-  if (int r = sort_particles(c, k, st, &perm, &skeys)) return r;
-  return deposit(c, k, perm, skeys, st);
+  unsigned* perm = nullptr;
+  if (int r = group_particles(c, k, st, &perm)) return r;
+  // deposit from a row-ordered copy of the positions (sequential reads of each row)
+  PM_CK(c->spos.ensure((size_t)3 * np * sizeof(float)), "alloc state");
+  PM_CK(launch_gather_state(positions, nullptr, np, perm, c->spos.as<float>(), nullptr, c->sms, st), "gather");
+  k.parts = abs_parts(c->spos.as<float>(), nullptr, np);
+  return deposit(c, k, nullptr, st);
 }
 
 int pm_fourier_grid(pm_ctx* c, float* fgrid, void* stream) {
@@ -313,13 +350,14 @@ int pm_integrate(pm_ctx* c, float* positions, float* velocities, long long np, d
   cudaStream_t st = (cudaStream_t)stream;
   Call k;
   k.sim = base_sim(c, np);
+  k.sim.xbits = 0;  // row keys: the kick reads the particles grouped by row (locality)
   k.sim.phi = const_cast<float*>(phi);
   set_kick(k.sim, a, f_a1, da);
   set_prefix(k, np, c->n);
   k.parts = abs_parts(positions, velocities, np);
   if (int r = upload(c, k, st)) return r;
-  unsigned *perm = nullptr, *skeys = nullptr;
-  if (int r = sort_particles(c, k, st, &perm, &skeys)) return r;
+  unsigned* perm = nullptr;
+  if (int r = group_particles(c, k, st, &perm)) return r;
   return kick(c, k, perm, st);
 }
 
@@ -335,13 +373,31 @@ int pm_advance_time(pm_ctx* c, const float* rho, float* positions, float* veloci
   return pm_integrate(c, positions, velocities, np, a, f_step(c, a, da), da, c->phi.as<float>(), stream);
 }
 
-int pm_step(pm_ctx* c, float* positions, float* velocities, long long np, double mass, double a, double da,
-            float* rho_out, void* stream) {
-  if (!c) return PM_ERR_ARG;
-  if (!positions || !velocities) return fail(c, PM_ERR_ARG, "null array");
-  if (int r = check_np(c, np)) return r;
-  if (!(a > 0.0)) return fail(c, PM_ERR_ARG, "scale factor must be positive");
-  cudaStream_t st = (cudaStream_t)stream;
+}  // extern "C"
+
+namespace {
+
+// Where a step reads and writes the caller's state.
+struct StepIO {
+  const float* pos_in;    // read once by the keys kernel (device-accessible: device or pinned host)
+  float* pos_copy;        // device copy the keys kernel leaves (null: pos_in is device memory)
+  const float* vel_in;    // device
+  cudaEvent_t vel_ready;  // vel_in complete (null: already)
+  float* pos_out;         // result in particle order (device or pinned host)
+  float* vel_out;
+  // pinned host velocities: copied to vel_in on `side` once the keys kernel has read the
+  // positions (the two transfers would share the link)
+  const float* vel_host = nullptr;
+  cudaStream_t side = nullptr;
+  cudaEvent_t keys_done = nullptr;
+};
+
+// src/pmesh.py:60-61 on absolute positions: keys -> counting sort by row -> row-ordered copy
+// of the state (the caller's arrays are in particle order, which scatters every row across
+// memory) -> deposit (fused with the x R2C when the density is not requested) -> Poisson
+// solve -> kick/drift in row order -> gathered back into particle order.
+int step_core(pm_ctx* c, const StepIO& io, long long np, double mass, double a, double da, float* rho_out,
+              cudaStream_t st) {
   const size_t gb = (size_t)c->n * c->n * c->n * sizeof(float);
   float* rho = rho_out;
   if (!rho) {
@@ -351,32 +407,75 @@ int pm_step(pm_ctx* c, float* positions, float* velocities, long long np, double
   PM_CK(c->phi.ensure(gb), "alloc phi");
   Call k;
   k.sim = base_sim(c, np);
+  k.sim.xbits = 0;  // row keys
   k.sim.rho = rho;
   k.sim.phi = c->phi.as<float>();
   k.sim.mass_scale = (float)(mass / (double)(1u << PM_FIX_BITS));
   set_green(c, k.sim, a);
   set_kick(k.sim, a, f_step(c, a, da), da);
   set_prefix(k, np, c->n);
-  k.parts = abs_parts(positions, velocities, np);
+  k.parts = abs_parts(const_cast<float*>(io.pos_in), nullptr, np);
   if (int r = prepare_spectral(c, k)) return r;
   if (int r = upload(c, k, st)) return r;
-  unsigned *perm = nullptr, *skeys = nullptr;
-  if (int r = sort_particles(c, k, st, &perm, &skeys)) return r;
+  const size_t pb = (size_t)3 * np * sizeof(float);
+  PM_CK(c->spos.ensure(pb), "alloc state");
+  PM_CK(c->svel.ensure(pb), "alloc state");
+  PM_CK(c->sort.ensure(np), "alloc sort");
+  unsigned* perm = nullptr;
+  unsigned* inv = c->sort.vals_alt.as<unsigned>();
+  if (int r = group_particles(c, k, st, &perm, inv, io.pos_copy)) return r;
+  if (io.vel_host) {
+    PM_CK(cudaEventRecord(io.keys_done, st), "event");
+    PM_CK(cudaStreamWaitEvent(io.side, io.keys_done, 0), "event");
+    PM_CK(cudaMemcpyAsync(const_cast<float*>(io.vel_in), io.vel_host, pb, cudaMemcpyHostToDevice, io.side),
+          "h2d velocities");
+    PM_CK(cudaEventRecord(io.vel_ready, io.side), "event");
+  }
+  PM_CK(launch_gather_state(io.pos_copy ? io.pos_copy : io.pos_in, nullptr, np, perm, c->spos.as<float>(), nullptr,
+                            c->sms, st),
+        "gather");
+  Parts sp = abs_parts(c->spos.as<float>(), c->svel.as<float>(), np);
+  k.parts = sp;
   if (!rho_out && deposit_r2c_supported(c->n)) {
     // the density is not requested: deposit straight into the x-transformed spectrum
-    const long long nrows = (long long)c->n * c->n;
-    PM_CK(c->row_start.ensure((nrows + 1) * sizeof(unsigned)), "alloc rows");
-    PM_CK(launch_row_start(skeys, np, k.sim.xbits, (unsigned)nrows, c->row_start.as<unsigned>(), st), "rows");
-    PM_CK(deposit_r2c_dispatch(c->n, c->d_sim.as<Sim>(), work(c, k, PH_DEP), k.parts, perm,
+    PM_CK(deposit_r2c_dispatch(c->n, c->d_sim.as<Sim>(), work(c, k, PH_DEP), sp, nullptr,
                                c->row_start.as<unsigned>(), POS_ABS, c->d_err.as<int>(),
                                grid_for(k.prefix[PH_DEP][1], c->sms, deposit_r2c_ctas_per_sm(c->n)), st),
           "fused deposit");
     if (int r = spectral(c, k, false, st, true)) return r;
-    return kick(c, k, perm, st);
+  } else {
+    if (int r = deposit(c, k, nullptr, st)) return r;
+    if (int r = spectral(c, k, false, st)) return r;
   }
-  if (int r = deposit(c, k, perm, skeys, st)) return r;
-  if (int r = spectral(c, k, false, st)) return r;
-  return kick(c, k, perm, st);
+  if (io.vel_ready) PM_CK(cudaStreamWaitEvent(st, io.vel_ready, 0), "wait velocities");
+  PM_CK(launch_gather_state(io.vel_in, nullptr, np, perm, c->svel.as<float>(), nullptr, c->sms, st), "gather");
+  if (int r = kick(c, k, nullptr, st)) return r;
+  PM_CK(launch_gather_state(c->spos.as<float>(), c->svel.as<float>(), np, inv, io.pos_out, io.vel_out, c->sms, st),
+        "gather back");
+  return PM_OK;
+}
+
+bool pinned_host(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pm_step(pm_ctx* c, float* positions, float* velocities, long long np, double mass, double a, double da,
+            float* rho_out, void* stream) {
+  if (!c) return PM_ERR_ARG;
+  if (!positions || !velocities) return fail(c, PM_ERR_ARG, "null array");
+  if (int r = check_np(c, np)) return r;
+  if (!(a > 0.0)) return fail(c, PM_ERR_ARG, "scale factor must be positive");
+  StepIO io{positions, nullptr, velocities, nullptr, positions, velocities};
+  return step_core(c, io, np, mass, a, da, rho_out, (cudaStream_t)stream);
 }
 
 int pm_step_host(pm_ctx* c, float* h_positions, float* h_velocities, long long np, double mass, double a,
@@ -384,15 +483,34 @@ int pm_step_host(pm_ctx* c, float* h_positions, float* h_velocities, long long n
   if (!c) return PM_ERR_ARG;
   if (!h_positions || !h_velocities) return fail(c, PM_ERR_ARG, "null array");
   if (int r = check_np(c, np)) return r;
+  if (!(a > 0.0)) return fail(c, PM_ERR_ARG, "scale factor must be positive");
   cudaStream_t st = (cudaStream_t)stream;
   const size_t pb = (size_t)3 * np * sizeof(float);
   PM_CK(c->hpos.ensure(pb), "alloc positions");
   PM_CK(c->hvel.ensure(pb), "alloc velocities");
-  PM_CK(cudaMemcpyAsync(c->hpos.p, h_positions, pb, cudaMemcpyHostToDevice, st), "h2d positions");
-  PM_CK(cudaMemcpyAsync(c->hvel.p, h_velocities, pb, cudaMemcpyHostToDevice, st), "h2d velocities");
-  if (int r = pm_step(c, c->hpos.as<float>(), c->hvel.as<float>(), np, mass, a, da, nullptr, stream)) return r;
-  PM_CK(cudaMemcpyAsync(h_positions, c->hpos.p, pb, cudaMemcpyDeviceToHost, st), "d2h positions");
-  PM_CK(cudaMemcpyAsync(h_velocities, c->hvel.p, pb, cudaMemcpyDeviceToHost, st), "d2h velocities");
+  if (pinned_host(h_positions) && pinned_host(h_velocities)) {
+    // Pinned arrays: the keys kernel reads the positions over the host link and leaves a
+    // device copy; the velocities then cross on a copy engine while the deposit and the
+    // solve run (the kick needs them first); the result is gathered back straight into the
+    // host arrays.
+    if (!c->side) {
+      PM_CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "side stream");
+      PM_CK(cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming), "event");
+      PM_CK(cudaEventCreateWithFlags(&c->ev_vel, cudaEventDisableTiming), "event");
+    }
+    StepIO io{h_positions, c->hpos.as<float>(), c->hvel.as<float>(), c->ev_vel, h_positions, h_velocities};
+    io.vel_host = h_velocities;
+    io.side = c->side;
+    io.keys_done = c->ev_start;
+    if (int r = step_core(c, io, np, mass, a, da, nullptr, st)) return r;
+  } else {  // pageable: copy engines both ways
+    PM_CK(cudaMemcpyAsync(c->hpos.p, h_positions, pb, cudaMemcpyHostToDevice, st), "h2d positions");
+    PM_CK(cudaMemcpyAsync(c->hvel.p, h_velocities, pb, cudaMemcpyHostToDevice, st), "h2d velocities");
+    StepIO io{c->hpos.as<float>(), nullptr, c->hvel.as<float>(), nullptr, c->hpos.as<float>(), c->hvel.as<float>()};
+    if (int r = step_core(c, io, np, mass, a, da, nullptr, st)) return r;
+    PM_CK(cudaMemcpyAsync(h_positions, c->hpos.p, pb, cudaMemcpyDeviceToHost, st), "d2h positions");
+    PM_CK(cudaMemcpyAsync(h_velocities, c->hvel.p, pb, cudaMemcpyDeviceToHost, st), "d2h velocities");
+  }
   PM_CK(cudaStreamSynchronize(st), "sync");
   return PM_OK;
 }

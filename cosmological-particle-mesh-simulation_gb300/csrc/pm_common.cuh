@@ -135,7 +135,7 @@ cudaError_t launch_power_spectrum(const float2* spec, int n, int pitch, int nbin
 
 // particle kernels
 cudaError_t launch_keys_abs(const Sim* sims, const Work& w, Parts p, unsigned* keys, unsigned* vals,
-                            int* err, int ctas, cudaStream_t st);
+                            int* err, int ctas, cudaStream_t st, Parts copy = Parts{});
 cudaError_t launch_keys_disp(const Sim* sims, const Work& w, Parts p, unsigned* keys, unsigned* vals,
                              int* err, int ctas, cudaStream_t st);
 cudaError_t launch_row_start(const unsigned* keys, long long n, int xbits, unsigned nrows,
@@ -147,6 +147,10 @@ constexpr int KICK_UNIT = 512;  // particles per work unit of the kick
 cudaError_t launch_kick(const Sim* sims, const Work& w, Parts in, Parts out, const unsigned* perm,
                         unsigned* keys_next, int mode, int* err, int ctas, cudaStream_t st);
 cudaError_t launch_coef(Sim* sims, int nsims, int advance, cudaStream_t st);
+// dst[k][j] = src[k][idx[j]] for the three rows of (3, np) positions (and velocities unless
+// vel is null)
+cudaError_t launch_gather_state(const float* pos, const float* vel, long long np, const unsigned* idx, float* spos,
+                                float* svel, int sms, cudaStream_t st);
 cudaError_t deposit_prepare();  // sets kernel attributes (call before graph capture)
 cudaError_t launch_abs_to_disp(const float* pos, const float* vel, long long np, int np1, int n,
                                const int* q_int, const float* q_frac, Parts out, long long off,

@@ -49,7 +49,8 @@ __device__ __forceinline__ bool source_cell(const Sim& S, const Parts& p, const 
 #pragma unroll
   for (int step = 16; step > 0; step >>= 1)
     if (r + step < NSRC && s_off[r + step] <= f) r += step;
-  const unsigned slot = __ldg(&perm[s_begin[r] + (f - s_off[r])]);
+  const unsigned pos = s_begin[r] + (f - s_off[r]);
+  const unsigned slot = perm ? __ldg(&perm[pos]) : pos;  // no permutation: the state is in row order
   c = particle_cell<MODE>(S, p, slot);
   const int n = S.n;
   int dy = c.y - y0, dz = c.z - z0;

@@ -23,10 +23,12 @@ constexpr int KEY_NT = 256;
 // ---------------------------------------------------------------------------------
 // keys
 // ---------------------------------------------------------------------------------
+// copy (POS_ABS, optional): the positions are also written there (the keys kernel reads
+// them once, e.g. from host memory, and leaves a device copy)
 template <int MODE>
 __global__ void __launch_bounds__(KEY_NT) k_keys(const Sim* __restrict__ sims, Work w, Parts p,
                                                  unsigned* __restrict__ keys,
-                                                 unsigned* __restrict__ vals, int* err) {
+                                                 unsigned* __restrict__ vals, int* err, Parts copy) {
   for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
     const int si = locate_sim(w, unit);
     const Sim& S = sims[si];
@@ -34,9 +36,19 @@ __global__ void __launch_bounds__(KEY_NT) k_keys(const Sim* __restrict__ sims, W
     if (i >= S.np) continue;
     const long long slot = S.part_off + i;
     // from the state itself (the cell records, if any, are written here)
-    Cell c = MODE == POS_ABS ? cell_abs(p.x[slot], p.y[slot], p.z[slot], S.n)
-                             : cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
-    if (MODE == POS_DISP && p.cell) store_cell_record(p, slot, c);
+    Cell c;
+    if (MODE == POS_ABS) {
+      const float x = p.x[slot], y = p.y[slot], z = p.z[slot];
+      if (copy.x) {
+        copy.x[slot] = x;
+        copy.y[slot] = y;
+        copy.z[slot] = z;
+      }
+      c = cell_abs(x, y, z, S.n);
+    } else {
+      c = cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
+      if (p.cell) store_cell_record(p, slot, c);
+    }
     if (!c.ok) { set_error(err, ERR_CELL_RANGE); c.x = c.y = c.z = 0; }
     keys[slot] = cell_key(S, c);
     if (vals) vals[slot] = (unsigned)slot;
@@ -226,7 +238,7 @@ __device__ __forceinline__ void kick_store(const Sim& S, const Parts& out, long 
 // Each thread advances KICK_PPT particles, KICK_NT apart: all their loads (state, then the
 // 32 potential taps each) are issued before any store, so that they overlap.
 template <int MODE>
-__global__ void __launch_bounds__(KICK_NT) k_kick(const Sim* __restrict__ sims, Work w, Parts in, Parts out,
+__global__ void __launch_bounds__(KICK_NT, 4) k_kick(const Sim* __restrict__ sims, Work w, Parts in, Parts out,
                                                   const unsigned* __restrict__ perm,
                                                   unsigned* __restrict__ keys_next, int* err) {
   for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
@@ -374,13 +386,13 @@ cudaError_t deposit_prepare() {
 size_t deposit_smem_bytes(int n, int ty, int tz) { return (size_t)n * ty * tz * sizeof(unsigned long long); }
 
 cudaError_t launch_keys_abs(const Sim* sims, const Work& w, Parts p, unsigned* keys, unsigned* vals,
-                            int* err, int ctas, cudaStream_t st) {
-  k_keys<POS_ABS><<<ctas, KEY_NT, 0, st>>>(sims, w, p, keys, vals, err);
+                            int* err, int ctas, cudaStream_t st, Parts copy) {
+  k_keys<POS_ABS><<<ctas, KEY_NT, 0, st>>>(sims, w, p, keys, vals, err, copy);
   return cudaGetLastError();
 }
 cudaError_t launch_keys_disp(const Sim* sims, const Work& w, Parts p, unsigned* keys, unsigned* vals,
                              int* err, int ctas, cudaStream_t st) {
-  k_keys<POS_DISP><<<ctas, KEY_NT, 0, st>>>(sims, w, p, keys, vals, err);
+  k_keys<POS_DISP><<<ctas, KEY_NT, 0, st>>>(sims, w, p, keys, vals, err, Parts{});
   return cudaGetLastError();
 }
 
@@ -411,6 +423,26 @@ cudaError_t launch_kick(const Sim* sims, const Work& w, Parts in, Parts out, con
                         unsigned* keys_next, int mode, int* err, int ctas, cudaStream_t st) {
   if (mode == POS_ABS) k_kick<POS_ABS><<<ctas, KICK_NT, 0, st>>>(sims, w, in, out, perm, keys_next, err);
   else k_kick<POS_DISP><<<ctas, KICK_NT, 0, st>>>(sims, w, in, out, perm, keys_next, err);
+  return cudaGetLastError();
+}
+
+// Absolute state in caller order <-> row order (drop-in step): sorted[j] = state[perm[j]],
+// and back, state[i] = sorted[inv[i]] -- gathers, so that the writes stay coalesced.  One
+// array per launch: the randomly read source (np floats) then stays in L2.
+__global__ void k_gather1(const float* __restrict__ src, long long np, const unsigned* __restrict__ idx,
+                          float* __restrict__ dst) {
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < np; j += (long long)gridDim.x * blockDim.x)
+    dst[j] = __ldg(&src[__ldg(&idx[j])]);
+}
+
+cudaError_t launch_gather_state(const float* pos, const float* vel, long long np, const unsigned* idx, float* spos,
+                                float* svel, int sms, cudaStream_t st) {
+  long long b = (np + 255) / 256;
+  if (b > (long long)sms * 16) b = (long long)sms * 16;
+  for (int k = 0; k < 3; ++k) {
+    k_gather1<<<(int)b, 256, 0, st>>>(pos + k * np, np, idx, spos + k * np);
+    if (vel) k_gather1<<<(int)b, 256, 0, st>>>(vel + k * np, np, idx, svel + k * np);
+  }
   return cudaGetLastError();
 }
 

@@ -263,3 +263,28 @@ def test_step_fused_deposit_matches_unfused(cuda):
         out.append((p.cpu().numpy(), v.cpu().numpy()))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("n_parts,n_cells", [(32, 64), (128, 256)])
+def test_step_host_pinned_and_pageable_match_device_step(cuda, n_parts, n_cells):
+    """pm_step_host on pinned arrays (positions read over the host link by the keys kernel,
+    the result gathered straight into host memory) and on pageable arrays (copy engines)
+    give the device step's bits."""
+    torch = cuda
+    from pmgpu.config import Config
+    from pmgpu import ics
+    cfg = Config(n_parts=n_parts, n_cells=n_cells, box_size=180.0, random_seed=6)
+    pos, vel = ics.initial_conditions(cfg)
+    ctx = ctx_for(cfg)
+    p, v = dev(torch, pos), dev(torch, vel)
+    hp = torch.from_numpy(pos.copy()).pin_memory()
+    hv = torch.from_numpy(vel.copy()).pin_memory()
+    pp, pv = pos.copy(), vel.copy()
+    for s in range(3):
+        a = cfg.a_init + s * cfg.da
+        ctx.step(p, v, cfg.mass, a, cfg.da)
+        ctx.step_host(hp, hv, cfg.mass, a, cfg.da)
+        ctx.step_host(pp, pv, cfg.mass, a, cfg.da)
+    ctx.check_device()
+    assert np.array_equal(hp.numpy(), p.cpu().numpy()) and np.array_equal(hv.numpy(), v.cpu().numpy())
+    assert np.array_equal(pp, p.cpu().numpy()) and np.array_equal(pv, v.cpu().numpy())
