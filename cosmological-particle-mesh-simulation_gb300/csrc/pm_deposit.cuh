@@ -1,8 +1,9 @@
 // Deterministic CIC deposit of one tile (density.py:7-48 of the reference).
 //
 // A tile is TZ x TY full x-rows.  The particles whose base cell lies in the tile's source
-// rows (the tile plus one row and one plane below, periodic) are found through the row
-// starts of the cell-key sort; their CIC weights that land inside the tile are added to
+// rows (the tile plus one row and one plane below, periodic: 7 runs of the row-sorted
+// order) are found through the row starts; their CIC weights that land inside the tile are
+// added to
 // integer accumulators in shared memory: weights quantised to 2^-26, a 32-bit low word
 // with carry into a 32-bit high word.  Integer sums do not depend on the order of the
 // atomics, so the deposit is bit-identical run to run.
@@ -25,18 +26,28 @@ __device__ __forceinline__ float fixed_to_float(unsigned l, unsigned h, float sc
 
 // Adds the 8 weights of a particle with base cell (cx, ly, lz) (ly, lz relative to the
 // tile, in [-1, TY-1] x [-1, TZ-1]) to the tile accumulators; tile row r of lo / hi starts
-// at word r * rs.
+// at word r * rs.  Corners outside the tile's rows are skipped (a neighbouring tile adds
+// them), unless the whole particle is inside.
 __device__ __forceinline__ void deposit_particle(unsigned* lo, unsigned* hi, int n, int rs, int cx, int ly, int lz,
                                                  const float (&wt)[8]) {
   const int x1 = cx + 1 == n ? 0 : cx + 1;
+  const bool inside = (unsigned)ly < (unsigned)(TY - 1) && (unsigned)lz < (unsigned)(TZ - 1);
+  const int base = (lz * TY + ly) * rs;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     const int ty2 = ly + corner_y(k), tz2 = lz + corner_z(k);
-    if (ty2 >= 0 && ty2 < TY && tz2 >= 0 && tz2 < TZ)
-      acc_add(lo, hi, (tz2 * TY + ty2) * rs + (corner_x(k) ? x1 : cx),
+    if (inside || (ty2 >= 0 && ty2 < TY && tz2 >= 0 && tz2 < TZ))
+      acc_add(lo, hi, base + (corner_z(k) * TY + corner_y(k)) * rs + (corner_x(k) ? x1 : cx),
               __float2uint_rn(wt[k] * (float)(1u << PM_FIX_BITS)));
   }
 }
+
+// Source ranges of a tile: the particles whose base cell lies in the tile's rows or one row
+// / plane below (periodic) are, in the row-sorted order, 7 runs of consecutive rows (rows
+// are numbered tile by tile, TZ x TY inside a tile):
+//   0: the tile itself (16 rows)            1: the tile below in z, its last plane (TY rows)
+//   2-5: the tile below in y, its last row of each plane    6: the diagonal tile, last row
+constexpr int NRUN = 7;
 
 // Base cell of source entry f relative to the tile; false if the entry is absent or bad.
 template <int MODE>
@@ -45,10 +56,10 @@ __device__ __forceinline__ bool source_cell(const Sim& S, const Parts& p, const 
                                             unsigned total, int y0, int z0, int* err, Cell& c, int& ly,
                                             int& lz) {
   if (f >= total) return false;
-  int r = 0;  // last source row with s_off[r] <= f
-#pragma unroll
-  for (int step = 16; step > 0; step >>= 1)
-    if (r + step < NSRC && s_off[r + step] <= f) r += step;
+  int r = 0;  // last run with s_off[r] <= f
+  if (s_off[4] <= f) r = 4;
+  if (s_off[r + 2] <= f) r += 2;
+  if (r + 1 < NRUN && s_off[r + 1] <= f) r += 1;
   const unsigned pos = s_begin[r] + (f - s_off[r]);
   const unsigned slot = perm ? __ldg(&perm[pos]) : pos;  // no permutation: the state is in row order
   c = particle_cell<MODE>(S, p, slot);
@@ -65,7 +76,7 @@ __device__ __forceinline__ bool source_cell(const Sim& S, const Parts& p, const 
 
 // Accumulate the tile at (y0, z0) of simulation S into lo/hi (TZ * TY rows of n cells,
 // row r at word r * rs of each; lo and hi together are 2 * TZ * TY * n contiguous words).
-// Entered and left by all NT threads, synchronised.
+// s_begin / s_off: NRUN + 1 words each.  Entered and left by all NT threads, synchronised.
 template <int MODE, int NT>
 __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
                                              const unsigned* __restrict__ row_start, int* err, int y0, int z0,
@@ -76,30 +87,38 @@ __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const
   uint4* z4 = reinterpret_cast<uint4*>(lo);
   for (int i = threadIdx.x; i < ncell / 2; i += NT) z4[i] = make_uint4(0u, 0u, 0u, 0u);
   if (warp == 0) {
-    // source rows (lz, ly) in [-1, TZ-1] x [-1, TY-1]: begin and an inclusive scan of counts
+    // first row and row count of every run, then an inclusive scan of the counts
     unsigned beg = 0, cnt = 0;
-    if (lane < NSRC) {
-      const int lz = lane / (TY + 1) - 1, ly = lane % (TY + 1) - 1;
-      const int z = z0 + lz < 0 ? z0 + lz + n : z0 + lz;
-      const int y = y0 + ly < 0 ? y0 + ly + n : y0 + ly;
-      const unsigned r = S.row_base + row_number(y, z, n);
-      beg = __ldg(&row_start[r]);
-      cnt = __ldg(&row_start[r + 1]) - beg;
+    if (lane < NRUN) {
+      const int ym = y0 == 0 ? n - TY : y0 - TY, zm = z0 == 0 ? n - TZ : z0 - TZ;  // tiles below
+      const int ntile_y = n / TY;
+      const unsigned t_own = (unsigned)(z0 / TZ) * ntile_y + y0 / TY;
+      const unsigned t_zb = (unsigned)(zm / TZ) * ntile_y + y0 / TY;
+      const unsigned t_yb = (unsigned)(z0 / TZ) * ntile_y + ym / TY;
+      const unsigned t_c = (unsigned)(zm / TZ) * ntile_y + ym / TY;
+      unsigned r0, nr;
+      if (lane == 0) { r0 = t_own * (TZ * TY); nr = TZ * TY; }
+      else if (lane == 1) { r0 = t_zb * (TZ * TY) + (TZ - 1) * TY; nr = TY; }
+      else if (lane < 6) { r0 = t_yb * (TZ * TY) + (lane - 2) * TY + TY - 1; nr = 1; }
+      else { r0 = t_c * (TZ * TY) + (TZ - 1) * TY + TY - 1; nr = 1; }
+      r0 += S.row_base;
+      beg = __ldg(&row_start[r0]);
+      cnt = __ldg(&row_start[r0 + nr]) - beg;
     }
     unsigned incl = cnt;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
+    for (int o = 1; o < 8; o <<= 1) {
       const unsigned t = __shfl_up_sync(FULL, incl, o);
       if (lane >= o) incl += t;
     }
-    if (lane < NSRC) {
+    if (lane < NRUN) {
       s_begin[lane] = beg;
       s_off[lane + 1] = incl;
     }
     if (lane == 0) s_off[0] = 0;
   }
   __syncthreads();
-  const unsigned total = s_off[NSRC];
+  const unsigned total = s_off[NRUN];
   // two source entries per lane and iteration, so that their loads overlap
   for (unsigned base = (unsigned)warp * 32u; base < total; base += 2 * NT) {
     Cell c0, c1;
