@@ -124,7 +124,7 @@ def measured_peak():
 def profiled_traffic():
     """Per-launch DRAM bytes (dram__bytes_read.sum + write.sum) of each phase's kernel from
     the committed ncu summary, scaled to the full workload there; None if absent."""
-    path = os.path.join(ROOT, "profiles", "kernels_512g_full.md")
+    path = os.path.join(ROOT, "profiles", "resident_step_256p_512g_launches.md")
     out = {}
     try:
         for line in open(path):
