@@ -111,6 +111,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+def max_over_ranks(x, dist=None, device="cpu"):
+    """The maximum of a per-rank float over all ranks: the slowest replica bounds the job."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
+def job_throughput(particles, steps, ranks, seconds):
+    """Whole-job particle-updates/s: every rank advances its own replica by `steps` steps."""
+    return particles * steps * ranks / seconds
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -218,12 +233,8 @@ def run_gpu(args, ws, rank, local):
         raise RuntimeError(f"ran {done} steps instead of {K}")
     b.close()
 
-    t_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = t.item()
-    value = np_ * K * ws / (t_max / 1e3)
+    t_max = max_over_ranks(ms, dist, "cuda")
+    value = job_throughput(np_, K, ws, t_max / 1e3)
 
     # ---- e2e: drop-in loop on host arrays through the C ABI -------------------------
     e2e = None
@@ -244,11 +255,8 @@ def run_gpu(args, ws, rank, local):
         torch.cuda.synchronize()
         te = time.perf_counter() - te0
         ctx.check_device()
-        if dist is not None:
-            t = torch.tensor([te], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = t.item()
-        e2e = {"value": np_ * args.e2e_steps * ws / te, "unit": UNIT,
+        te = max_over_ranks(te, dist, "cuda")
+        e2e = {"value": job_throughput(np_, args.e2e_steps, ws, te), "unit": UNIT,
                "h2d_bytes_per_step": 2 * 3 * 4 * np_, "d2h_bytes_per_step": 2 * 3 * 4 * np_,
                "steps": args.e2e_steps, "api": "pm_step_host (C ABI, pinned host arrays)"}
         ctx.close()
