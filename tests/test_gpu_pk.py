@@ -171,3 +171,37 @@ def test_device_power_spectrum_rejects_bad_arguments(cuda):
     with pytest.raises(_lib.PMError):
         ctx.power_spectrum(rho, box_size=-1.0)
     ctx.close()
+
+
+@pytest.mark.slow
+def test_config3_512p_1024g_short_run_against_fp64(cuda):
+    """The 512^3-particle / 1024^3-grid configuration (box 500 Mpc/h, seed 1): initial
+    conditions on the device, 5 resident steps, against the float64 copy of the reference
+    algorithm from the same initial conditions."""
+    torch = cuda
+    from oracle import torch64 as T
+    from pmgpu.batch import Batch
+    from pmgpu.config import Config
+    from pmgpu.device_ics import DeviceICs
+    cfg = Config(n_parts=512, n_cells=1024, box_size=500.0, random_seed=1, steps=500)
+    g = DeviceICs(512)
+    pos, vel = g.generate(cfg)
+    g.close()
+    b = Batch()
+    sid = b.add(cfg, pos, vel)
+    b.step(5)
+    b.check_device()
+    gp, gv, a_gpu, done = b.get(sid, device=True)
+    b.close()
+    assert done == 5
+    p64, v64, a64 = T.run(pos, vel, cfg, 5)
+    assert abs(a64 - a_gpu) < 1e-12
+    n = cfg.n_cells
+    d = torch.remainder(gp.double() - p64, float(n))
+    assert torch.minimum(d, n - d).max().item() < 1e-2
+    assert ((gv.double() - v64).norm() / v64.norm()).item() < 5e-4
+    del d, gv, v64
+    k, pk_gpu, _ = T.power_spectrum(T.density(gp.double(), cfg.mass, n), cfg.box_size)
+    _, pk_64, _ = T.power_spectrum(T.density(p64, cfg.mass, n), cfg.box_size)
+    sel = np.arange(1, len(k) + 1) < n // 4
+    assert np.abs(pk_gpu[sel] / pk_64[sel] - 1.0).max() < 1e-3
