@@ -15,13 +15,17 @@ namespace pm {
 constexpr int DEP_NT = 512;
 constexpr int DEP_ROW_NT = 256;  // fused deposit with the register row transform
 
-__device__ __forceinline__ void acc_add(unsigned* lo, unsigned* hi, int i, unsigned q) {
-  const unsigned old = atomicAdd(&lo[i], q);
-  if (old + q < old) atomicAdd(&hi[i], 1u);
+constexpr int COARSE_SHIFT = 12;
+
+__device__ __forceinline__ void acc_add(unsigned* lo, unsigned* co, int i, unsigned q) {
+  atomicAdd(&lo[i], q);  // results unused: non-returning shared-memory reductions
+  atomicAdd(&co[i], q >> COARSE_SHIFT);
 }
 
-__device__ __forceinline__ float fixed_to_float(unsigned l, unsigned h, float scale) {
-  return (h == 0u ? __uint2float_rn(l) : __ull2float_rn(((unsigned long long)h << 32) | l)) * scale;
+// The exact sum from its low word and its coarse sum, times scale.
+__device__ __forceinline__ float fixed_to_float(unsigned l, unsigned c, float scale) {
+  const unsigned long long est = (unsigned long long)c << COARSE_SHIFT;
+  return __ull2float_rn(est + (unsigned)(l - (unsigned)est)) * scale;
 }
 
 // Adds the 8 weights of a particle with base cell (cx, ly, lz) (ly, lz relative to the

@@ -30,9 +30,11 @@ __host__ __device__ constexpr int cx_rows(int n) {
   // rows of the x passes per CTA: ~SP_ELEMS complex, a multiple of 8, at most n*n
   return (SP_ELEMS / (n / 2)) / 8 * 8 > n * n ? n * n : (SP_ELEMS / (n / 2)) / 8 * 8;
 }
-__host__ __device__ constexpr int cline_width(int n) { return n >= 768 ? 8 : 16; }
+// columns of a line-pass bundle: 8 from n = 512 up (for 512 one bundle of 32 KB per stage,
+// two CTAs per SM)
+__host__ __device__ constexpr int cline_width(int n) { return n >= 512 ? 8 : 16; }
 __host__ __device__ constexpr int cline_bpc(int n) {
-  return SP_ELEMS / (n * cline_width(n)) < 1 ? 1 : SP_ELEMS / (n * cline_width(n));
+  return n == 512 ? 1 : (SP_ELEMS / (n * cline_width(n)) < 1 ? 1 : SP_ELEMS / (n * cline_width(n)));
 }
 __host__ __device__ constexpr int chalf(int n) { return n / 2 + 1; }
 __host__ __device__ constexpr int cbundles_per_plane(int n) {
@@ -43,9 +45,10 @@ __host__ __device__ constexpr int cpitch(int n) { return (chalf(n) + 15) / 16 * 
 // Line passes that stream through a TMA ring: boxes of at most 256 rows tiling n.
 __host__ __device__ constexpr int line_box_rows(int n) { return n <= 256 ? n : (n % 256 == 0 ? 256 : n / 2); }
 __host__ __device__ constexpr bool tma_lines(int n) { return n >= 32 && line_box_rows(n) <= 256; }
-// Threads of a line-pass CTA: 512 (pairs of lines, up to 128 registers); the radix-3 sizes
-// from 192 up, transformed line by line, run 1024.
-__host__ __device__ constexpr int line_nt(int n) { return n % 3 == 0 && n >= 192 ? 1024 : 512; }
+// Threads of a line-pass CTA: 512 (pairs of lines, up to 128 registers), 256 for n = 512
+// (two CTAs per SM); the radix-3 sizes from 192 up, transformed line by line, run 1024.
+__host__ __device__ constexpr int line_nt(int n) { return n == 512 ? 256 : (n % 3 == 0 && n >= 192 ? 1024 : 512); }
+__host__ __device__ constexpr int line_ctas_per_sm(int n) { return n == 512 ? 2 : 1; }
 constexpr int XTMA_NT = 1024;  // x passes
 constexpr int TMA_STAGES = 3;
 __host__ __device__ constexpr size_t tma_stage_bytes(int n) {
@@ -366,7 +369,7 @@ struct GreenEpi {
 
 // MODE 0: y forward, 1: y inverse, 2: z Green, 3: z Green (caller table), 4: z forward, 5: z inverse
 template <int N, int MODE>
-__global__ void __launch_bounds__(line_nt(N), 1) k_line_tma(const CUtensorMap* __restrict__ maps,
+__global__ void __launch_bounds__(line_nt(N), line_ctas_per_sm(N)) k_line_tma(const CUtensorMap* __restrict__ maps,
                                                         const Sim* __restrict__ sims, Work w, int* err) {
   constexpr int BW = cline_width(N), BPC = cline_bpc(N), NL = BW * BPC;
   constexpr int BOX = line_box_rows(N), NBOX = N / BOX;
@@ -899,6 +902,8 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
   if constexpr (tma_lines(N)) {
     if (maps) {
       const size_t sm = tma_smem_bytes(N);
+      const int lcap = line_ctas_per_sm(N) * device_sms();
+      const int grid = w.total < lcap ? w.total : lcap;
       switch (kind) {
         case SPEC_Y_FWD: k_line_tma<N, 0><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
         case SPEC_Y_INV: k_line_tma<N, 1><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
