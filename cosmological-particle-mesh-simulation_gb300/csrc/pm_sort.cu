@@ -266,19 +266,29 @@ constexpr int CS_NT = 256;
 constexpr int SCAN_TILE = 4096;  // rows per block of the row-start scan
 constexpr int SCAN_IPT = SCAN_TILE / CS_NT;
 
+// UNR batches of 32 keys per warp and iteration: their loads, matches and atomics overlap.
+constexpr int CS_UNR = 4;
+
 __global__ void __launch_bounds__(CS_NT) k_row_hist(const unsigned* __restrict__ keys, long long n, unsigned nrows,
                                                     unsigned* __restrict__ count, int* err) {
   const int lane = threadIdx.x & 31;
-  const long long stride = (long long)gridDim.x * CS_NT;
-  for (long long b = (long long)blockIdx.x * CS_NT + (threadIdx.x & ~31); b < n; b += stride) {
-    const long long i = b + lane;
-    unsigned k = i < n ? __ldg(&keys[i]) : 0xffffffffu;
-    if (i < n && k >= nrows) {
-      set_error(err, ERR_CELL_RANGE);
-      k = nrows - 1;
+  const long long stride = (long long)gridDim.x * CS_NT * CS_UNR;
+  for (long long b = ((long long)blockIdx.x * CS_NT + (threadIdx.x & ~31)) * CS_UNR; b < n; b += stride) {
+    unsigned k[CS_UNR];
+#pragma unroll
+    for (int u = 0; u < CS_UNR; ++u) {
+      const long long i = b + u * 32 + lane;
+      k[u] = i < n ? __ldg(&keys[i]) : 0xffffffffu;
+      if (i < n && k[u] >= nrows) {
+        set_error(err, ERR_CELL_RANGE);
+        k[u] = nrows - 1;
+      }
     }
-    const unsigned grp = __match_any_sync(0xffffffffu, k);
-    if (k != 0xffffffffu && lane == __ffs(grp) - 1) atomicAdd(&count[k], (unsigned)__popc(grp));
+#pragma unroll
+    for (int u = 0; u < CS_UNR; ++u) {
+      const unsigned grp = __match_any_sync(0xffffffffu, k[u]);
+      if (k[u] != 0xffffffffu && lane == __ffs(grp) - 1) atomicAdd(&count[k[u]], (unsigned)__popc(grp));
+    }
   }
 }
 
@@ -355,19 +365,31 @@ __global__ void __launch_bounds__(CS_NT) k_row_scatter(const unsigned* __restric
   const long long nwarps = (long long)gridDim.x * (CS_NT / 32);
   for (long long c = (long long)blockIdx.x * (CS_NT / 32) + (threadIdx.x >> 5); c < nchunks; c += nwarps) {
     const long long end = (c + 1) * SCATTER_CHUNK < n ? (c + 1) * SCATTER_CHUNK : n;
-    for (long long b = c * SCATTER_CHUNK; b < end; b += 32) {
-      const long long i = b + lane;
-      unsigned k = i < end ? __ldg(&keys[i]) : 0xffffffffu;
-      if (i < end && k >= nrows) k = nrows - 1;
-      const unsigned grp = __match_any_sync(0xffffffffu, k);
-      const int leader = __ffs(grp) - 1;
-      unsigned pos = 0;
-      if (k != 0xffffffffu && lane == leader) pos = atomicAdd(&cursor[k], (unsigned)__popc(grp));
-      pos = __shfl_sync(0xffffffffu, pos, leader);
-      if (k != 0xffffffffu) {
-        const unsigned p = pos + __popc(grp & ((1u << lane) - 1u));
-        perm[p] = (unsigned)i;
-        if (inv) inv[i] = p;
+    for (long long b = c * SCATTER_CHUNK; b < end; b += 32 * CS_UNR) {
+      // CS_UNR batches in order: a row's cursor is advanced batch by batch (program order of
+      // the same address), and the batches' atomics are in flight together
+      unsigned k[CS_UNR], grp[CS_UNR], pos[CS_UNR];
+#pragma unroll
+      for (int u = 0; u < CS_UNR; ++u) {
+        const long long i = b + u * 32 + lane;
+        k[u] = i < end ? __ldg(&keys[i]) : 0xffffffffu;
+        if (i < end && k[u] >= nrows) k[u] = nrows - 1;
+      }
+#pragma unroll
+      for (int u = 0; u < CS_UNR; ++u) {
+        grp[u] = __match_any_sync(0xffffffffu, k[u]);
+        pos[u] = 0;
+        if (k[u] != 0xffffffffu && lane == __ffs(grp[u]) - 1) pos[u] = atomicAdd(&cursor[k[u]], (unsigned)__popc(grp[u]));
+      }
+#pragma unroll
+      for (int u = 0; u < CS_UNR; ++u) {
+        const unsigned p0 = __shfl_sync(0xffffffffu, pos[u], __ffs(grp[u]) - 1);
+        if (k[u] != 0xffffffffu) {
+          const long long i = b + u * 32 + lane;
+          const unsigned p = p0 + __popc(grp[u] & ((1u << lane) - 1u));
+          perm[p] = (unsigned)i;
+          if (inv) inv[i] = p;
+        }
       }
     }
   }
@@ -383,7 +405,7 @@ cudaError_t row_counting_sort(const unsigned* keys, long long n, unsigned nrows,
   if (nrows == 0) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(count, 0, (size_t)nrows * sizeof(unsigned), st);
   if (e) return e;
-  long long want = (n + CS_NT - 1) / CS_NT;
+  long long want = (n + CS_NT * CS_UNR - 1) / (CS_NT * CS_UNR);
   const int ctas = (int)(want < (long long)sms * 8 ? (want > 0 ? want : 1) : (long long)sms * 8);
   k_row_hist<<<ctas, CS_NT, 0, st>>>(keys, n, nrows, count, err);
   const int nb = (int)row_sort_block_sums(nrows);
