@@ -118,6 +118,66 @@ template <bool INV> struct DFT<16, INV> {
   }
 };
 
+// Composite DFT of R = R1 R2 points in registers: j = R2 a + b, k = c + R1 d; an R1-point DFT
+// over a for each b, twiddles w_R^(b c) (forward exp(-2 pi i m / R)), an R2-point DFT over b.
+// WR::w(m) gives w_R^m for the forward direction.
+template <int R1, int R2, class WR, bool INV>
+__device__ __forceinline__ void dft_composite(float2* v) {
+  float2 t[R2][R1];
+#pragma unroll
+  for (int b = 0; b < R2; ++b) {
+    float2 x[R1];
+#pragma unroll
+    for (int a = 0; a < R1; ++a) x[a] = v[R2 * a + b];
+    DFT<R1, INV>::run(x);
+#pragma unroll
+    for (int c = 0; c < R1; ++c) {
+      if (b * c == 0) {
+        t[b][c] = x[c];
+      } else {
+        float2 w = WR::w((b * c) % (R1 * R2));
+        if (INV) w.y = -w.y;
+        t[b][c] = cmul(x[c], w);
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < R1; ++c) {
+    float2 y[R2];
+#pragma unroll
+    for (int b = 0; b < R2; ++b) y[b] = t[b][c];
+    DFT<R2, INV>::run(y);
+#pragma unroll
+    for (int d = 0; d < R2; ++d) v[c + R1 * d] = y[d];
+  }
+}
+
+// exp(-2 pi i m / 12) and exp(-2 pi i m / 24): multiples of 30 and 15 degrees
+struct W12 {
+  static __device__ __forceinline__ float2 w(int m) {
+    const float h = 0.5f, r = 0.866025403784438646763723f;  // cos 60, cos 30
+    const float c[12] = {1.f, r, h, 0.f, -h, -r, -1.f, -r, -h, 0.f, h, r};
+    const float s[12] = {0.f, h, r, 1.f, r, h, 0.f, -h, -r, -1.f, -r, -h};
+    return make_float2(c[m], -s[m]);
+  }
+};
+struct W24 {
+  static __device__ __forceinline__ float2 w(int m) {
+    const float a = 0.965925826289068286749743f, b = 0.258819045102520762348898f;  // cos, sin 15
+    const float h = 0.5f, r = 0.866025403784438646763723f, q = 0.707106781186547524400844f;
+    const float c[24] = {1.f, a, r, q, h, b, 0.f, -b, -h, -q, -r, -a, -1.f, -a, -r, -q, -h, -b, 0.f, b, h, q, r, a};
+    const float s[24] = {0.f, b, h, q, r, a, 1.f, a, r, q, h, b, 0.f, -b, -h, -q, -r, -a, -1.f, -a, -r, -q, -h, -b};
+    return make_float2(c[m], -s[m]);
+  }
+};
+
+template <bool INV> struct DFT<12, INV> {
+  static __device__ __forceinline__ void run(float2* v) { dft_composite<3, 4, W12, INV>(v); }
+};
+template <bool INV> struct DFT<24, INV> {
+  static __device__ __forceinline__ void run(float2* v) { dft_composite<3, 8, W24, INV>(v); }
+};
+
 // ---------------------------------------------------------------------------------
 // Radix plans (product of radices == L)
 // ---------------------------------------------------------------------------------

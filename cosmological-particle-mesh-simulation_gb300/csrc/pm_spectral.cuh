@@ -58,12 +58,25 @@ __host__ __device__ constexpr size_t tma_smem_bytes(int n) { return TMA_STAGES *
 
 // x passes with the row transform in registers (power-of-two n, 64 <= n <= 512): a row of
 // M = n/2 complex points is factored M = P x Q and held by T lanes of a warp
-__host__ __device__ constexpr bool xrow_ok(int n) { return n == 64 || n == 128 || n == 256 || n == 512; }
-__host__ __device__ constexpr int xrow_P(int n) { return n >= 256 ? 16 : 8; }
+// (n: P x Q, T) -- 64: 8x4, 4; 128: 8x8, 8; 256: 16x8, 8; 512: 16x16, 16;
+// 96: 12x4, 4; 192: 12x8, 4; 384: 24x8, 8
+__host__ __device__ constexpr bool xrow_ok(int n) {
+  return n == 64 || n == 128 || n == 256 || n == 512 || n == 96 || n == 192 || n == 384;
+}
+__host__ __device__ constexpr int xrow_P(int n) { return n % 3 == 0 ? (n == 384 ? 24 : 12) : (n >= 256 ? 16 : 8); }
 __host__ __device__ constexpr int xrow_Q(int n) { return n / 2 / xrow_P(n); }
-__host__ __device__ constexpr int xrow_T(int n) { return xrow_Q(n) < xrow_P(n) ? xrow_Q(n) : xrow_P(n); }
+__host__ __device__ constexpr int xrow_T(int n) {
+  return n == 192 ? 4 : (xrow_Q(n) < xrow_P(n) ? xrow_Q(n) : xrow_P(n));
+}
 __host__ __device__ constexpr int xrow_rows_per_warp(int n) { return 32 / xrow_T(n); }
-constexpr int XR_NT = 256;
+// threads of a row-transform CTA: up to 8 warps, their exchange buffers within 40 KB of
+// static shared memory
+__host__ __device__ constexpr int xrow_warp_bytes(int n) {
+  return xrow_rows_per_warp(n) * xrow_Q(n) * (xrow_P(n) + 1) * 8;
+}
+__host__ __device__ constexpr int xrow_nt(int n) {
+  return 32 * (40960 / xrow_warp_bytes(n) < 8 ? (40960 / xrow_warp_bytes(n) < 1 ? 1 : 40960 / xrow_warp_bytes(n)) : 8);
+}
 
 // x passes fed by bulk copies into a double-buffered staging area (one simulation per launch)
 __host__ __device__ constexpr bool tma_rows(int n);
@@ -525,7 +538,8 @@ __device__ __forceinline__ void xrow_untangle_store(const float2 (&o)[xrow_P(N) 
 }
 
 template <int N, bool C2R>
-__global__ void __launch_bounds__(XR_NT) k_x_row(const Sim* __restrict__ sims, Work w) {
+__global__ void __launch_bounds__(xrow_nt(N)) k_x_row(const Sim* __restrict__ sims, Work w) {
+  constexpr int XR_NT = xrow_nt(N);
   constexpr int M = N / 2, P = xrow_P(N), Q = xrow_Q(N), T = xrow_T(N), RPW = 32 / T;
   constexpr int RB = Q * (P + 1);  // exchange buffer of a row (>= M + 1)
   constexpr int NB1 = Q / T, NB2 = P / T;
@@ -885,10 +899,10 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
   const int grid = w.total < device_sms() ? w.total : device_sms();
   if constexpr (xrow_ok(N)) {
     if (kind == SPEC_X_R2C || kind == SPEC_X_C2R) {
-      const int per = XR_NT / 32, want = (w.total + per - 1) / per, cap = device_sms() * 8;
+      const int per = xrow_nt(N) / 32, want = (w.total + per - 1) / per, cap = device_sms() * 8;
       const int g = want < cap ? want : cap;
-      if (kind == SPEC_X_R2C) k_x_row<N, false><<<g, XR_NT, 0, st>>>(sims, w);
-      else k_x_row<N, true><<<g, XR_NT, 0, st>>>(sims, w);
+      if (kind == SPEC_X_R2C) k_x_row<N, false><<<g, xrow_nt(N), 0, st>>>(sims, w);
+      else k_x_row<N, true><<<g, xrow_nt(N), 0, st>>>(sims, w);
       return cudaGetLastError();
     }
   }

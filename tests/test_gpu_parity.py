@@ -203,7 +203,7 @@ def test_nonfinite_position_flagged(cuda):
 
 
 # ---- larger sizes: oracle comparison and size-independent properties ----------------------
-@pytest.mark.parametrize("nparts,ncells", [(64, 128), (96, 192), (128, 256)])
+@pytest.mark.parametrize("nparts,ncells", [(48, 96), (64, 128), (96, 192), (128, 256), (192, 384)])
 def test_density_potential_large(cuda, nparts, ncells):
     torch = cuda
     from pmgpu.config import Config
