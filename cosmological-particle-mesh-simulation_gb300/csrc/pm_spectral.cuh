@@ -30,11 +30,15 @@ __host__ __device__ constexpr int cx_rows(int n) {
   // rows of the x passes per CTA: ~SP_ELEMS complex, a multiple of 8, at most n*n
   return (SP_ELEMS / (n / 2)) / 8 * 8 > n * n ? n * n : (SP_ELEMS / (n / 2)) / 8 * 8;
 }
-// columns of a line-pass bundle: 8 from n = 512 up (for 512 one bundle of 32 KB per stage,
-// two CTAs per SM)
-__host__ __device__ constexpr int cline_width(int n) { return n >= 512 ? 8 : 16; }
+// Line passes of the 512 grid run two CTAs per SM, each with 32 KB TMA
+// stages of bundles 8 columns wide; the others one CTA with 64 KB stages.
+__host__ __device__ constexpr bool line_small(int n) { return n == 512; }
+// columns of a line-pass bundle
+__host__ __device__ constexpr int cline_width(int n) { return n >= 512 || line_small(n) ? 8 : 16; }
+// bundles per unit (per TMA stage)
 __host__ __device__ constexpr int cline_bpc(int n) {
-  return n == 512 ? 1 : (SP_ELEMS / (n * cline_width(n)) < 1 ? 1 : SP_ELEMS / (n * cline_width(n)));
+  return line_small(n) ? SP_ELEMS / 2 / (n * 8)
+                       : (SP_ELEMS / (n * cline_width(n)) < 1 ? 1 : SP_ELEMS / (n * cline_width(n)));
 }
 __host__ __device__ constexpr int chalf(int n) { return n / 2 + 1; }
 __host__ __device__ constexpr int cbundles_per_plane(int n) {
@@ -45,10 +49,12 @@ __host__ __device__ constexpr int cpitch(int n) { return (chalf(n) + 15) / 16 * 
 // Line passes that stream through a TMA ring: boxes of at most 256 rows tiling n.
 __host__ __device__ constexpr int line_box_rows(int n) { return n <= 256 ? n : (n % 256 == 0 ? 256 : n / 2); }
 __host__ __device__ constexpr bool tma_lines(int n) { return n >= 32 && line_box_rows(n) <= 256; }
-// Threads of a line-pass CTA: 512 (pairs of lines, up to 128 registers), 256 for n = 512
-// (two CTAs per SM); the radix-3 sizes from 192 up, transformed line by line, run 1024.
-__host__ __device__ constexpr int line_nt(int n) { return n == 512 ? 256 : (n % 3 == 0 && n >= 192 ? 1024 : 512); }
-__host__ __device__ constexpr int line_ctas_per_sm(int n) { return n == 512 ? 2 : 1; }
+// Threads of a line-pass CTA: 512 (pairs of lines, up to 128 registers), 256 for the
+// two-CTA sizes; the radix-3 sizes from 192 up, transformed line by line, run 1024.
+__host__ __device__ constexpr int line_nt(int n) {
+  return line_small(n) ? 256 : (n % 3 == 0 && n >= 192 ? 1024 : 512);
+}
+__host__ __device__ constexpr int line_ctas_per_sm(int n) { return line_small(n) ? 2 : 1; }
 constexpr int XTMA_NT = 1024;  // x passes
 constexpr int TMA_STAGES = 3;
 __host__ __device__ constexpr size_t tma_stage_bytes(int n) {
