@@ -330,9 +330,10 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
   Parts in = state(b, cur), out = state(b, 1 - cur);
   // group the particles by x-row: row starts and the permutation to row order
   unsigned* perm = b->sort.vals.as<unsigned>();
+  // (the row histogram of the keys was made by the previous kick, or by ensure_keys)
   PB_CK(row_counting_sort(b->sort.keys.as<unsigned>(), P.ptot, P.rows, b->row_count.as<unsigned>(),
                           b->row_start.as<unsigned>(), b->row_cursor.as<unsigned>(), b->scan_sums.as<unsigned>(),
-                          perm, err, b->sms, st),
+                          perm, err, b->sms, st, nullptr, true),
         "sort");
   PB_CK(mark(1 + PP_SORT), "event");
   PB_CK(mark(1 + PP_ROWS), "event");  // the row starts come out of the counting sort
@@ -363,8 +364,10 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
     }
     PB_CK(mark(1 + PP_X_R2C + o), "event");
   }
+  // the kick writes the next keys and counts them per row for the next step's sort
+  PB_CK(cudaMemsetAsync(b->row_count.p, 0, sizeof(unsigned) * (size_t)P.rows, st), "count reset");
   PB_CK(launch_kick(ds, work_of(b, PH_KICK, P.fixed_total[PH_KICK]), in, out, perm, b->sort.keys.as<unsigned>(),
-                    POS_DISP, err, grid_for(P.fixed_total[PH_KICK], b->sms, 16), st),
+                    POS_DISP, err, grid_for(P.fixed_total[PH_KICK], b->sms, 16), st, b->row_count.as<unsigned>()),
         "kick");
   PB_CK(mark(1 + PP_KICK), "event");
   PB_CK(launch_coef(b->d_sims.as<Sim>(), P.nsims, 1, st), "coef");
@@ -375,8 +378,9 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
 // Kernel launches of one step for the current plan.
 int launches_per_step(pm_batch* b) {
   const Plan& P = b->plan;
-  // counting sort: histogram, 3 scan kernels, scatter (the count reset is a memset)
-  int n = 5 + (P.fixed_total[PH_DEP] > 0 ? 1 : 0) + 5 * (int)P.sizes.size() + 1 + 1;
+  // counting sort: 3 scan kernels and the scatter (the kick makes the histogram; the count
+  // reset is a memset)
+  int n = 4 + (P.fixed_total[PH_DEP] > 0 ? 1 : 0) + 5 * (int)P.sizes.size() + 1 + 1;
   return n;  // each fused size replaces its x R2C launch by the fused deposit
 }
 
@@ -387,6 +391,9 @@ int ensure_keys(pm_batch* b, cudaStream_t st) {
                          b->sort.keys.as<unsigned>(), nullptr, b->d_err.as<int>(),
                          grid_for(P.fixed_total[PH_KEYS], b->sms, 16), st),
         "keys");
+  PB_CK(row_histogram(b->sort.keys.as<unsigned>(), P.ptot, P.rows, b->row_count.as<unsigned>(), b->d_err.as<int>(),
+                      b->sms, st),
+        "row histogram");
   b->keys_valid = true;
   return PM_OK;
 }

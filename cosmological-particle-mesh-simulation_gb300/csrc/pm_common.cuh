@@ -144,8 +144,10 @@ cudaError_t launch_deposit(const Sim* sims, const Work& w, Parts p, const unsign
                            const unsigned* row_start, int mode, int* err, int ctas, size_t smem,
                            cudaStream_t st);
 constexpr int KICK_UNIT = 512;  // particles per work unit of the kick
+// row_count (displacement mode, with keys_next): the kick also counts the next keys per row
 cudaError_t launch_kick(const Sim* sims, const Work& w, Parts in, Parts out, const unsigned* perm,
-                        unsigned* keys_next, int mode, int* err, int ctas, cudaStream_t st);
+                        unsigned* keys_next, int mode, int* err, int ctas, cudaStream_t st,
+                        unsigned* row_count = nullptr);
 cudaError_t launch_coef(Sim* sims, int nsims, int advance, cudaStream_t st);
 // dst[k][j] = src[k][idx[j]] for the three rows of (3, np) positions (and velocities unless
 // vel is null)
@@ -179,9 +181,13 @@ cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int begin_bi
 // counts) and perm[j] = index of the j-th key in row order (order inside a row not
 // specified).  Scratch: count and cursor (nrows each), block_sums (row_sort_block_sums).
 size_t row_sort_block_sums(unsigned nrows);
-// inv (optional): inv[i] = sorted position of key i.
+// inv (optional): inv[i] = sorted position of key i.  counted: count already holds the
+// row histogram of keys (else it is zeroed and computed here).
 cudaError_t row_counting_sort(const unsigned* keys, long long n, unsigned nrows, unsigned* count,
                               unsigned* row_start, unsigned* cursor, unsigned* block_sums, unsigned* perm, int* err,
-                              int sms, cudaStream_t st, unsigned* inv = nullptr);
+                              int sms, cudaStream_t st, unsigned* inv = nullptr, bool counted = false);
+// count[r] = number of keys equal to r (count zeroed first)
+cudaError_t row_histogram(const unsigned* keys, long long n, unsigned nrows, unsigned* count, int* err, int sms,
+                          cudaStream_t st);
 
 }  // namespace pm

@@ -200,9 +200,10 @@ __device__ __forceinline__ void gather_force(const float* __restrict__ phi, int 
   gather_taps(GlobalRows(phi, n, c.y, c.z), n, c, g);
 }
 
-// Kick/drift of one particle whose state and force are in registers; writes it out.
+// Kick/drift of one particle whose state and force are in registers; writes it out and
+// returns its next key (resident mode with keys_next; else 0xffffffff).
 template <int MODE>
-__device__ __forceinline__ void kick_store(const Sim& S, const Parts& out, long long sp, long long slot, float px,
+__device__ __forceinline__ unsigned kick_store(const Sim& S, const Parts& out, long long sp, long long slot, float px,
                                            float py, float pz, float vx, float vy, float vz, unsigned id,
                                            const float (&g)[3], unsigned* __restrict__ keys_next, int* err) {
   const float kk = S.kick, dr = S.drift;
@@ -230,17 +231,23 @@ __device__ __forceinline__ void kick_store(const Sim& S, const Parts& out, long 
       Cell cn = cell_disp(S, id, nx, ny, nz);
       if (out.cell) store_cell_record(out, sp, cn);
       if (!cn.ok) { set_error(err, ERR_CELL_RANGE); cn.x = cn.y = cn.z = 0; }
-      keys_next[sp] = cell_key(S, cn);
+      const unsigned key = cell_key(S, cn);
+      keys_next[sp] = key;
+      return key;
     }
   }
+  return 0xffffffffu;
 }
 
 // Each thread advances KICK_PPT particles, KICK_NT apart: all their loads (state, then the
 // 32 potential taps each) are issued before any store, so that they overlap.
 template <int MODE>
+// row_count (optional, with keys_next): histogram of the next keys, for the next step's
+// counting sort
 __global__ void __launch_bounds__(KICK_NT, 4) k_kick(const Sim* __restrict__ sims, Work w, Parts in, Parts out,
                                                   const unsigned* __restrict__ perm,
-                                                  unsigned* __restrict__ keys_next, int* err) {
+                                                  unsigned* __restrict__ keys_next, int* err,
+                                                  unsigned* __restrict__ row_count) {
   for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
     const int si = locate_sim(w, unit);
     const Sim& S = sims[si];
@@ -271,12 +278,22 @@ __global__ void __launch_bounds__(KICK_NT, 4) k_kick(const Sim* __restrict__ sim
       g[q][0] = g[q][1] = g[q][2] = 0.f;
       if (slot[q] >= 0 && c[q].ok) gather_force(S.phi, S.n, c[q], g[q]);
     }
+    unsigned key[KICK_PPT];
 #pragma unroll
     for (int q = 0; q < KICK_PPT; ++q) {
+      key[q] = 0xffffffffu;
       if (slot[q] < 0) continue;
       if (!c[q].ok) set_error(err, ERR_CELL_RANGE);
-      kick_store<MODE>(S, out, sp[q], slot[q], px[q], py[q], pz[q], vx[q], vy[q], vz[q], id[q], g[q], keys_next,
-                       err);
+      key[q] = kick_store<MODE>(S, out, sp[q], slot[q], px[q], py[q], pz[q], vx[q], vy[q], vz[q], id[q], g[q],
+                                keys_next, err);
+    }
+    if (row_count) {  // the whole warp takes part: equal keys are counted once per warp
+      const int lane = threadIdx.x & 31;
+#pragma unroll
+      for (int q = 0; q < KICK_PPT; ++q) {
+        const unsigned grp = __match_any_sync(0xffffffffu, key[q]);
+        if (key[q] != 0xffffffffu && lane == __ffs(grp) - 1) atomicAdd(&row_count[key[q]], (unsigned)__popc(grp));
+      }
     }
   }
 }
@@ -420,9 +437,9 @@ cudaError_t launch_deposit(const Sim* sims, const Work& w, Parts p, const unsign
 }
 
 cudaError_t launch_kick(const Sim* sims, const Work& w, Parts in, Parts out, const unsigned* perm,
-                        unsigned* keys_next, int mode, int* err, int ctas, cudaStream_t st) {
-  if (mode == POS_ABS) k_kick<POS_ABS><<<ctas, KICK_NT, 0, st>>>(sims, w, in, out, perm, keys_next, err);
-  else k_kick<POS_DISP><<<ctas, KICK_NT, 0, st>>>(sims, w, in, out, perm, keys_next, err);
+                        unsigned* keys_next, int mode, int* err, int ctas, cudaStream_t st, unsigned* row_count) {
+  if (mode == POS_ABS) k_kick<POS_ABS><<<ctas, KICK_NT, 0, st>>>(sims, w, in, out, perm, keys_next, err, nullptr);
+  else k_kick<POS_DISP><<<ctas, KICK_NT, 0, st>>>(sims, w, in, out, perm, keys_next, err, row_count);
   return cudaGetLastError();
 }
 

@@ -399,15 +399,25 @@ __global__ void __launch_bounds__(CS_NT) k_row_scatter(const unsigned* __restric
 
 size_t row_sort_block_sums(unsigned nrows) { return ((size_t)nrows + SCAN_TILE - 1) / SCAN_TILE; }
 
-cudaError_t row_counting_sort(const unsigned* keys, long long n, unsigned nrows, unsigned* count,
-                              unsigned* row_start, unsigned* cursor, unsigned* block_sums, unsigned* perm, int* err,
-                              int sms, cudaStream_t st, unsigned* inv) {
+cudaError_t row_histogram(const unsigned* keys, long long n, unsigned nrows, unsigned* count, int* err, int sms,
+                          cudaStream_t st) {
   if (nrows == 0) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(count, 0, (size_t)nrows * sizeof(unsigned), st);
   if (e) return e;
   long long want = (n + CS_NT * CS_UNR - 1) / (CS_NT * CS_UNR);
   const int ctas = (int)(want < (long long)sms * 8 ? (want > 0 ? want : 1) : (long long)sms * 8);
   k_row_hist<<<ctas, CS_NT, 0, st>>>(keys, n, nrows, count, err);
+  return cudaGetLastError();
+}
+
+cudaError_t row_counting_sort(const unsigned* keys, long long n, unsigned nrows, unsigned* count,
+                              unsigned* row_start, unsigned* cursor, unsigned* block_sums, unsigned* perm, int* err,
+                              int sms, cudaStream_t st, unsigned* inv, bool counted) {
+  if (nrows == 0) return cudaErrorInvalidValue;
+  if (!counted) {
+    cudaError_t e = row_histogram(keys, n, nrows, count, err, sms, st);
+    if (e) return e;
+  }
   const int nb = (int)row_sort_block_sums(nrows);
   k_scan_reduce<<<nb, CS_NT, 0, st>>>(count, nrows, block_sums);
   k_scan_top<<<1, CS_NT, 0, st>>>(block_sums, nb);
