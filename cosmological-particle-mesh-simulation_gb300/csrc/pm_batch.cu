@@ -6,7 +6,7 @@
 // the state back in the order of the step's cell-key sort, so that the next step reads
 // it almost in order.  Simulation s owns the slot range [part_off_s, part_off_s + np_s)
 // and the x-rows [row_base_s, row_base_s + N_s^2) of the common key space, in the same
-// order, so one radix sort serves the whole batch.  Every phase is one persistent launch
+// order, so one counting sort over the rows serves the whole batch.  Every phase is one launch
 // over all simulations (the spectral phases: one per distinct grid size).  A step is
 // captured once into a CUDA graph per plan and replayed; the scale factor and the
 // step coefficients advance on the device.
