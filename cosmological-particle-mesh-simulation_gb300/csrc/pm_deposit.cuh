@@ -78,49 +78,65 @@ __device__ __forceinline__ bool source_cell(const Sim& S, const Parts& p, const 
   return ok;
 }
 
+// The 7 runs of the tile at (y0, z0): lane r < NRUN loads the first sorted index and the
+// particle count of run r.
+struct RunLoad {
+  unsigned beg, cnt;
+};
+
+__device__ __forceinline__ RunLoad run_load(const Sim& S, const unsigned* __restrict__ row_start, int y0, int z0,
+                                            int lane) {
+  RunLoad v{0u, 0u};
+  if (lane < NRUN) {
+    const int n = S.n;
+    const int ym = y0 == 0 ? n - TY : y0 - TY, zm = z0 == 0 ? n - TZ : z0 - TZ;  // tiles below
+    const int ntile_y = n / TY;
+    const unsigned t_own = (unsigned)(z0 / TZ) * ntile_y + y0 / TY;
+    const unsigned t_zb = (unsigned)(zm / TZ) * ntile_y + y0 / TY;
+    const unsigned t_yb = (unsigned)(z0 / TZ) * ntile_y + ym / TY;
+    const unsigned t_c = (unsigned)(zm / TZ) * ntile_y + ym / TY;
+    unsigned r0, nr;
+    if (lane == 0) { r0 = t_own * (TZ * TY); nr = TZ * TY; }
+    else if (lane == 1) { r0 = t_zb * (TZ * TY) + (TZ - 1) * TY; nr = TY; }
+    else if (lane < 6) { r0 = t_yb * (TZ * TY) + (lane - 2) * TY + TY - 1; nr = 1; }
+    else { r0 = t_c * (TZ * TY) + (TZ - 1) * TY + TY - 1; nr = 1; }
+    r0 += S.row_base;
+    v.beg = __ldg(&row_start[r0]);
+    v.cnt = __ldg(&row_start[r0 + nr]) - v.beg;
+  }
+  return v;
+}
+
+// Warp-wide: the run table (first sorted index, and the inclusive scan of the counts).
+__device__ __forceinline__ void run_table(const RunLoad& v, int lane, unsigned* s_begin, unsigned* s_off) {
+  unsigned incl = v.cnt;
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    const unsigned t = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane < NRUN) {
+    s_begin[lane] = v.beg;
+    s_off[lane + 1] = incl;
+  }
+  if (lane == 0) s_off[0] = 0;
+}
+
 // Accumulate the tile at (y0, z0) of simulation S into lo/hi (TZ * TY rows of n cells,
 // row r at word r * rs of each; lo and hi together are 2 * TZ * TY * n contiguous words).
-// s_begin / s_off: NRUN + 1 words each.  Entered and left by all NT threads, synchronised.
+// s_begin / s_off: NRUN + 1 words each, already holding the tile's run table when
+// runs_ready.  Entered and left by all NT threads, synchronised.
 template <int MODE, int NT>
 __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
                                              const unsigned* __restrict__ row_start, int* err, int y0, int z0,
-                                             unsigned* lo, unsigned* hi, int rs, unsigned* s_begin, unsigned* s_off) {
+                                             unsigned* lo, unsigned* hi, int rs, unsigned* s_begin, unsigned* s_off,
+                                             bool runs_ready = false) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n = S.n;
   const int ncell = TZ * TY * n;  // zero 2 * ncell words
   uint4* z4 = reinterpret_cast<uint4*>(lo);
   for (int i = threadIdx.x; i < ncell / 2; i += NT) z4[i] = make_uint4(0u, 0u, 0u, 0u);
-  if (warp == 0) {
-    // first row and row count of every run, then an inclusive scan of the counts
-    unsigned beg = 0, cnt = 0;
-    if (lane < NRUN) {
-      const int ym = y0 == 0 ? n - TY : y0 - TY, zm = z0 == 0 ? n - TZ : z0 - TZ;  // tiles below
-      const int ntile_y = n / TY;
-      const unsigned t_own = (unsigned)(z0 / TZ) * ntile_y + y0 / TY;
-      const unsigned t_zb = (unsigned)(zm / TZ) * ntile_y + y0 / TY;
-      const unsigned t_yb = (unsigned)(z0 / TZ) * ntile_y + ym / TY;
-      const unsigned t_c = (unsigned)(zm / TZ) * ntile_y + ym / TY;
-      unsigned r0, nr;
-      if (lane == 0) { r0 = t_own * (TZ * TY); nr = TZ * TY; }
-      else if (lane == 1) { r0 = t_zb * (TZ * TY) + (TZ - 1) * TY; nr = TY; }
-      else if (lane < 6) { r0 = t_yb * (TZ * TY) + (lane - 2) * TY + TY - 1; nr = 1; }
-      else { r0 = t_c * (TZ * TY) + (TZ - 1) * TY + TY - 1; nr = 1; }
-      r0 += S.row_base;
-      beg = __ldg(&row_start[r0]);
-      cnt = __ldg(&row_start[r0 + nr]) - beg;
-    }
-    unsigned incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 8; o <<= 1) {
-      const unsigned t = __shfl_up_sync(FULL, incl, o);
-      if (lane >= o) incl += t;
-    }
-    if (lane < NRUN) {
-      s_begin[lane] = beg;
-      s_off[lane + 1] = incl;
-    }
-    if (lane == 0) s_off[0] = 0;
-  }
+  if (warp == 0 && !runs_ready) run_table(run_load(S, row_start, y0, z0, lane), lane, s_begin, s_off);
   __syncthreads();
   const unsigned total = s_off[NRUN];
   // two source entries per lane and iteration, so that their loads overlap

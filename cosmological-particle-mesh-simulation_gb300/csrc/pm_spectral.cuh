@@ -773,12 +773,14 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
   unsigned* hi = lo + HO;
   float2* F = reinterpret_cast<float2*>(acc_raw);
   float* Ff = reinterpret_cast<float*>(acc_raw);
+  bool runs_ready = false;  // the run table of this tile was loaded during the previous one
   for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
     const int si = locate_sim(w, unit);
     const Sim& S = sims[si];
     const int local = unit - __ldg(&w.prefix[si]);
     const int y0 = (local % (N / TY)) * TY, z0 = (local / (N / TY)) * TZ;
-    deposit_tile<MODE, NT>(S, p, perm, row_start, err, y0, z0, lo, hi, RS, s_begin, s_off);
+    deposit_tile<MODE, NT>(S, p, perm, row_start, err, y0, z0, lo, hi, RS, s_begin, s_off, runs_ready);
+    runs_ready = false;
     const float ms = S.mass_scale;
     if constexpr (xrow_ok(N)) {
       // the tile's NL rows: T lanes per row, rows r = warp * RPW + sub; the row's exchange
@@ -802,11 +804,26 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
             const uint2 ll = l2[j], hh = h2[j];
             v2[i][a] = make_float2(fixed_to_float(ll.x, hh.x, ms), fixed_to_float(ll.y, hh.y, ms));
           }
+        // warp 0 loads the next tile's run table now and stores it after the transform,
+        // so that the loads' latency hides behind it (the table is free: the particle loop
+        // of this tile is over)
+        const int next = unit + gridDim.x;
+        RunLoad nl{0u, 0u};
+        int nsi = 0, ny0 = 0, nz0 = 0;
+        if (threadIdx.x < 32 && next < w.total) {
+          nsi = locate_sim(w, next);
+          const int nloc = next - __ldg(&w.prefix[nsi]);
+          ny0 = (nloc % (N / TY)) * TY;
+          nz0 = (nloc / (N / TY)) * TZ;
+          nl = run_load(sims[nsi], row_start, ny0, nz0, lane);
+        }
         xrow_transform<N, false>(v2, o2, rb, t, S.tw);
         const long long row = (long long)(z0 + r / TY) * N + (y0 + r % TY);
         xrow_untangle_store<N>(o2, rb, t, S.tw, S.spec + row * S.pitch);
+        if (threadIdx.x < 32 && next < w.total) run_table(nl, lane, s_begin, s_off);
       }
       __syncthreads();
+      runs_ready = true;
       continue;
     }
     float v[PER];
