@@ -12,8 +12,8 @@ steps are the first K steps of that run.
   roofline  the phase with the largest share of the step, from CUDA events recorded on
           the launch stream around each phase (pm_batch_profile), against its
           algorithmic bytes.
-  cpu_baseline  the FP64 numpy/scipy port of the reference path (oracle/) on the host
-          cores, one bounded sample of full-size steps.
+  cpu_baseline  the CPU port of the reference step (oracle/: C + OpenMP particle loops,
+          scipy.fft) on all host cores, one bounded sample of full-size steps.
 
 ``--impl reference`` times only that CPU port (the reference itself needs numba and
 pyFFTW, which are not installed) and prints its own line.  With torchrun and N > 1 each
@@ -300,24 +300,27 @@ def run_gpu(args, ws, rank, local):
 
 
 def cpu_baseline(cfg, pos, vel, steps):
-    """FP64 numpy/scipy port of the reference step (oracle/) on all host cores."""
+    """The reference step on all host cores: the C + OpenMP restatement of its particle
+    loops (oracle/cpu_step.c, float64 arithmetic on the float32 state, threads over
+    particles like the reference's numba prange) and scipy.fft for the Poisson solve."""
     import numpy as np
-    from oracle import pm_oracle as O
     cores = len(os.sched_getaffinity(0))
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    from oracle import cpu_port as C
+    from oracle import pm_oracle as O
+    C.load()
     fg = O.fourier_grid(cfg.n_cells)
-    p, v = pos.astype(np.float32), vel.astype(np.float32)
+    p, v = np.array(pos, dtype=np.float32), np.array(vel, dtype=np.float32)
     a = cfg.a_init
     t0 = time.perf_counter()
     for _ in range(steps):
-        rho = O.density(p, cfg.mass, cfg.n_cells)
-        x, vv = O.advance_time(rho, p, v, fg, a, cfg.da, cfg.omega_m0, cfg.omega_lambda0, cfg.omega_k0, cfg.h0,
-                               workers=cores)
-        p, v = x.astype(np.float32), vv.astype(np.float32)
+        C.step(p, v, cfg.mass, a, cfg.da, cfg, fg, workers=cores)
         a += cfg.da
     t = time.perf_counter() - t0
     return {"value": cfg.np_total * steps / t, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{steps} full-size step(s) (256^3 particles, 512^3 grid) of the FP64 numpy/scipy port, "
-                      f"FFTs on {cores} threads, particle loops vectorised single-threaded",
+            "sample": f"{steps} full-size step(s) ({cfg.n_parts}^3 particles, {cfg.n_cells}^3 grid) of the CPU port "
+                      f"of the reference step: particle loops in C + OpenMP on {cores} threads, FFTs in scipy.fft "
+                      f"(complex128) on {cores} threads",
             "seconds": round(t, 2)}
 
 
@@ -449,8 +452,9 @@ def run_reference(args, ws, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded GRF + Zel'dovich ICs (reference algorithm)",
             "config": {"workload": WORKLOAD, "n_parts": 256, "n_cells": 512, "box_size": 250.0,
-                       "note": "numba/pyFFTW are not installed: the reference path runs as its FP64 "
-                               "numpy/scipy port; steps bounded to a few full-size steps"},
+                       "note": "numba/pyFFTW are not installed: the reference step runs as its CPU port "
+                               "(C + OpenMP particle loops, scipy.fft, all host cores); steps bounded to a few "
+                               "full-size steps"},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
