@@ -468,7 +468,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--profile-steps", type=int, default=5)
-    ap.add_argument("--cpu-steps", type=int, default=1)
+    # full-size CPU steps timed (about 1.7 s each on 16 Arm cores: a 10 s sample)
+    ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-parts", type=int, default=256, help="reduced cases for profiling only")
     ap.add_argument("--n-cells", type=int, default=512)
