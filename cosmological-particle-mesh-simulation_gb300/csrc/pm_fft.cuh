@@ -351,6 +351,111 @@ __device__ __forceinline__ void fft_passes_pairs(float2* s, const float2* __rest
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Forward transform, a pointwise map, inverse transform (the z pass of the Poisson solve).
+//
+// The last forward pass (radix R, stride NS = L / R) leaves in each thread the R outputs
+// j + r L / R of one line (or pair of lines): exactly the inputs of the first pass of an
+// inverse transform whose first radix is also R.  The inverse therefore runs the plan in
+// reverse order (its first radix is the forward's last), and the two passes meet in
+// registers -- the map is applied between them -- instead of through shared memory: one
+// shared-memory round trip and two barriers fewer per transform pair.
+// ---------------------------------------------------------------------------------
+template <int L, int P, bool REV>
+__host__ __device__ constexpr int plan_radix() {
+  return REV ? Plan<L>::r[Plan<L>::np - 1 - P] : Plan<L>::r[P];
+}
+
+// Passes P .. PEND-1 of the plan (reversed with REV), entered with stride NS.
+template <int L, int P, int PEND, int NS, int NL, int BW, int NT, bool INV, bool REV>
+__device__ __forceinline__ void passes_span(float2* s, const float2* __restrict__ tw, int tws) {
+  if constexpr (P < PEND) {
+    constexpr int R = plan_radix<L, P, REV>();
+    if constexpr (blocked_pairs(L))
+      stockham_pass_pairs<L, R, NS, NL, BW, NT, INV>(s, tw, tws);
+    else
+      stockham_pass<L, R, NS, NL, Blocked<L, BW>, NT, INV>(s, tw, tws);
+    passes_span<L, P + 1, PEND, NS * R, NL, BW, NT, INV, REV>(s, tw, tws);
+  }
+}
+
+// The turn: last forward pass, `epi` on each output (element e of line), first inverse pass.
+template <int L, int R, int NL, int BW, int NT, class EPI>
+__device__ __forceinline__ void stockham_turn(float2* s, const float2* __restrict__ tw, int tws, const EPI& epi) {
+  using LAY = Blocked<L, BW>;
+  constexpr int NS = L / R;  // forward stride of the last pass == the inverse's block count
+  constexpr bool PAIRS = blocked_pairs(L);
+  constexpr int NG = PAIRS ? NL / 2 : NL;  // line groups: pairs of lines, or lines
+  constexpr int NTASK = NG * NS;
+  constexpr int TPT = (NTASK + NT - 1) / NT;
+  float4* s4 = reinterpret_cast<float4*>(s);
+  float2 a[TPT][R], b[TPT][R];
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    const int task = threadIdx.x + t * NT;
+    if ((NTASK % NT) == 0 || task < NTASK) {
+      const int line = PAIRS ? 2 * (task % NG) : task % NG, j = task / NG;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if constexpr (PAIRS) {
+          const float4 q = s4[LAY::at(j + r * NS, line) >> 1];
+          a[t][r] = make_float2(q.x, q.y);
+          b[t][r] = make_float2(q.z, q.w);
+        } else {
+          a[t][r] = s[LAY::at(j + r * NS, line)];
+        }
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    const int task = threadIdx.x + t * NT;
+    if ((NTASK % NT) == 0 || task < NTASK) {
+      const int line = PAIRS ? 2 * (task % NG) : task % NG, j = task / NG;
+      // forward: k = j (j < NS); the twiddle index r k L / (NS R) = r k
+      if (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          const float2 w = __ldg(&tw[(r * j) * tws]);
+          a[t][r] = cmul(a[t][r], w);
+          if constexpr (PAIRS) b[t][r] = cmul(b[t][r], w);
+        }
+      }
+      DFT<R, false>::run(a[t]);
+      if constexpr (PAIRS) DFT<R, false>::run(b[t]);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        a[t][r] = epi(a[t][r], j + r * NS, line);
+        if constexpr (PAIRS) b[t][r] = epi(b[t][r], j + r * NS, line + 1);
+      }
+      // inverse, first pass (stride 1: no twiddles), outputs j R + r
+      DFT<R, true>::run(a[t]);
+      if constexpr (PAIRS) DFT<R, true>::run(b[t]);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if constexpr (PAIRS)
+          s4[LAY::at(j * R + r, line) >> 1] = make_float4(a[t][r].x, a[t][r].y, b[t][r].x, b[t][r].y);
+        else
+          s[LAY::at(j * R + r, line)] = a[t][r];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Unnormalised forward DFT of NL lines (Blocked layout), `epi` on every spectral value
+// (element j of line), unnormalised inverse DFT.  Entered by all NT threads after a
+// __syncthreads(); returns synchronised.
+template <int L, int NL, int BW, int NT, class EPI>
+__device__ __forceinline__ void fft_lines_blocked_turn(float2* s, const float2* __restrict__ tw, int tws,
+                                                       const EPI& epi) {
+  constexpr int NPL = Plan<L>::np, RL = Plan<L>::r[NPL - 1];
+  passes_span<L, 0, NPL - 1, 1, NL, BW, NT, false, false>(s, tw, tws);
+  stockham_turn<L, RL, NL, BW, NT>(s, tw, tws, epi);
+  passes_span<L, 1, NPL, RL, NL, BW, NT, true, true>(s, tw, tws);
+}
+
 // Unnormalised DFT of NL interleaved lines of length L held in shared memory.
 // Must be entered by all NT threads after a __syncthreads(); returns synchronised.
 template <int L, int NL, int LS, int NT, bool INV>

@@ -456,10 +456,9 @@ __global__ void __launch_bounds__(line_nt(N), line_ctas_per_sm(N)) k_line_tma(co
     } else if (MODE == 1 || MODE == 5) {
       fft_lines_blocked<N, NL, BW, line_nt(N), true>(s, S.tw, 1);
     } else {
-      // forward z transform; the Green function is applied as the last pass stores
+      // forward z transform, the Green function, inverse z transform (meeting in registers)
       const GreenEpi<N, MODE == 3> epi{S.green, S.s2, S.fgrid, b0, cnt};
-      fft_lines_blocked<N, NL, BW, line_nt(N), false>(s, S.tw, 1, epi);
-      fft_lines_blocked<N, NL, BW, line_nt(N), true>(s, S.tw, 1);
+      fft_lines_blocked_turn<N, NL, BW, line_nt(N)>(s, S.tw, 1, epi);
     }
     fence_proxy_async_smem();
     __syncthreads();
