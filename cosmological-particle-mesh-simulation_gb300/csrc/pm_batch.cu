@@ -238,6 +238,7 @@ int build_plan(pm_batch* b, cudaStream_t st) {
     Lattice* l = lattice_for(b, r.np1, r.n);
     d.q_int = l->qi.as<int>();
     d.q_frac = l->qf.as<float>();
+    d.q_step = r.np1 > 0 && r.n % r.np1 == 0 ? r.n / r.np1 : 0;
     d.mass_scale = (float)(std::pow((double)r.n / r.np1, 3) / (double)(1u << PM_FIX_BITS));
     d.a = r.a;
     d.da = r.da;

@@ -66,17 +66,23 @@ __device__ __forceinline__ int wrap_int(int c, int n) {
 //   cell = (q_int + floor(q_frac + d)) mod n,  offset = (q_frac + d) - floor(q_frac + d)
 __device__ __forceinline__ Cell cell_disp(const Sim& S, unsigned id, float dx, float dy, float dz) {
   const unsigned ix = id >> 20, iy = (id >> 10) & 1023u, iz = id & 1023u;
-  const float sx = __ldg(&S.q_frac[ix]) + dx;
-  const float sy = __ldg(&S.q_frac[iy]) + dy;
-  const float sz = __ldg(&S.q_frac[iz]) + dz;
+  // integer lattice step (np1 divides n): q_int = q_step i and q_frac = 1/2 exactly, the
+  // same values the tables hold, without the tables' scattered loads
+  const int qs = S.q_step;
+  const float sx = (qs ? 0.5f : __ldg(&S.q_frac[ix])) + dx;
+  const float sy = (qs ? 0.5f : __ldg(&S.q_frac[iy])) + dy;
+  const float sz = (qs ? 0.5f : __ldg(&S.q_frac[iz])) + dz;
   const float lx = floorf(sx), ly = floorf(sy), lz = floorf(sz);
   Cell c;
   c.ok = isfinite(sx) && isfinite(sy) && isfinite(sz) && fabsf(lx) < 1e8f && fabsf(ly) < 1e8f &&
          fabsf(lz) < 1e8f;
   const int n = S.n;
-  c.x = c.ok ? wrap_int(__ldg(&S.q_int[ix]) + (int)lx, n) : 0;
-  c.y = c.ok ? wrap_int(__ldg(&S.q_int[iy]) + (int)ly, n) : 0;
-  c.z = c.ok ? wrap_int(__ldg(&S.q_int[iz]) + (int)lz, n) : 0;
+  const int qx = qs ? qs * (int)ix : __ldg(&S.q_int[ix]);
+  const int qy = qs ? qs * (int)iy : __ldg(&S.q_int[iy]);
+  const int qz = qs ? qs * (int)iz : __ldg(&S.q_int[iz]);
+  c.x = c.ok ? wrap_int(qx + (int)lx, n) : 0;
+  c.y = c.ok ? wrap_int(qy + (int)ly, n) : 0;
+  c.z = c.ok ? wrap_int(qz + (int)lz, n) : 0;
   c.fx = sx - lx; c.fy = sy - ly; c.fz = sz - lz;
   return c;
 }

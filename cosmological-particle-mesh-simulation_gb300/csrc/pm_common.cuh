@@ -36,7 +36,7 @@ struct Sim {
   int xbits;        // bits of x in the cell key
   int ty, tz;       // deposit tile: tz planes x ty rows of full x-rows
   int flags;
-  int pad0;
+  int q_step;       // n / np1 when np1 divides n (lattice q = q_step i + 1/2); 0: use the tables
   long long np;        // particle count
   long long part_off;  // first particle slot in the batch particle arrays
   unsigned row_base;   // first global row number of this simulation

@@ -53,19 +53,24 @@ __device__ __forceinline__ void deposit_particle(unsigned* lo, unsigned* hi, int
 //   2-5: the tile below in y, its last row of each plane    6: the diagonal tile, last row
 constexpr int NRUN = 7;
 
-// Base cell of source entry f relative to the tile; false if the entry is absent or bad.
-template <int MODE>
-__device__ __forceinline__ bool source_cell(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
-                                            const unsigned* s_begin, const unsigned* s_off, unsigned f,
-                                            unsigned total, int y0, int z0, int* err, Cell& c, int& ly,
-                                            int& lz) {
-  if (f >= total) return false;
+// Slot of source entry f (0xffffffff past the end): its run, its place in the row-sorted
+// order, and the permutation.
+__device__ __forceinline__ unsigned source_slot(const unsigned* __restrict__ perm, const unsigned* s_begin,
+                                                const unsigned* s_off, unsigned f, unsigned total) {
+  if (f >= total) return 0xffffffffu;
   int r = 0;  // last run with s_off[r] <= f
   if (s_off[4] <= f) r = 4;
   if (s_off[r + 2] <= f) r += 2;
   if (r + 1 < NRUN && s_off[r + 1] <= f) r += 1;
   const unsigned pos = s_begin[r] + (f - s_off[r]);
-  const unsigned slot = perm ? __ldg(&perm[pos]) : pos;  // no permutation: the state is in row order
+  return perm ? __ldg(&perm[pos]) : pos;  // no permutation: the state is in row order
+}
+
+// Base cell of the source particle in `slot` relative to the tile; false if absent or bad.
+template <int MODE>
+__device__ __forceinline__ bool slot_cell(const Sim& S, const Parts& p, unsigned slot, int y0, int z0, int* err,
+                                          Cell& c, int& ly, int& lz) {
+  if (slot == 0xffffffffu) return false;
   c = particle_cell<MODE>(S, p, slot);
   const int n = S.n;
   int dy = c.y - y0, dz = c.z - z0;
@@ -139,13 +144,19 @@ __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const
   if (warp == 0 && !runs_ready) run_table(run_load(S, row_start, y0, z0, lane), lane, s_begin, s_off);
   __syncthreads();
   const unsigned total = s_off[NRUN];
-  // two source entries per lane and iteration, so that their loads overlap
-  for (unsigned base = (unsigned)warp * 32u; base < total; base += 2 * NT) {
+  // two source entries per lane and iteration, so that their loads overlap; the slots (the
+  // permutation loads) of the next iteration are fetched before this one's cells
+  unsigned base = (unsigned)warp * 32u;
+  unsigned sl0 = source_slot(perm, s_begin, s_off, base + lane, total);
+  unsigned sl1 = source_slot(perm, s_begin, s_off, base + NT + lane, total);
+  for (; base < total; base += 2 * NT) {
+    const unsigned nb = base + 2 * NT;
+    const unsigned nx0 = source_slot(perm, s_begin, s_off, nb + lane, total);
+    const unsigned nx1 = source_slot(perm, s_begin, s_off, nb + NT + lane, total);
     Cell c0, c1;
     int ly0 = 0, lz0 = 0, ly1 = 0, lz1 = 0;
-    const bool ok0 = source_cell<MODE>(S, p, perm, s_begin, s_off, base + lane, total, y0, z0, err, c0, ly0, lz0);
-    const bool ok1 =
-        source_cell<MODE>(S, p, perm, s_begin, s_off, base + NT + lane, total, y0, z0, err, c1, ly1, lz1);
+    const bool ok0 = slot_cell<MODE>(S, p, sl0, y0, z0, err, c0, ly0, lz0);
+    const bool ok1 = slot_cell<MODE>(S, p, sl1, y0, z0, err, c1, ly1, lz1);
     if (ok0) {
       float wt[8];
       cic_weights(c0, wt);
@@ -156,6 +167,8 @@ __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const
       cic_weights(c1, wt);
       deposit_particle(lo, hi, n, rs, c1.x, ly1, lz1, wt);
     }
+    sl0 = nx0;
+    sl1 = nx1;
   }
   __syncthreads();
 }
