@@ -118,6 +118,43 @@ __device__ __forceinline__ Cell particle_cell(const Sim& S, const Parts& p, long
   return cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
 }
 
+// The same in two steps, so that the loads can be issued early: the four words the cell is
+// made from (record: cell word and offsets; displacement: id and d; absolute: x, y, z),
+// then the cell.  present false: no particle (the words are not loaded).
+struct RawCell {
+  unsigned w;
+  float a, b, c;
+  bool present;
+};
+
+template <int MODE>
+__device__ __forceinline__ RawCell load_raw_cell(const Parts& p, unsigned slot) {
+  RawCell r{0u, 0.f, 0.f, 0.f, slot != 0xffffffffu};
+  if (!r.present) return r;
+  if (MODE == POS_DISP && p.cell) {
+    r.w = p.cell[slot]; r.a = p.fx[slot]; r.b = p.fy[slot]; r.c = p.fz[slot];
+  } else {
+    if (MODE == POS_DISP) r.w = p.id[slot];
+    r.a = p.x[slot]; r.b = p.y[slot]; r.c = p.z[slot];
+  }
+  return r;
+}
+
+template <int MODE>
+__device__ __forceinline__ Cell raw_cell(const Sim& S, const Parts& p, const RawCell& r) {
+  if (MODE == POS_ABS) return cell_abs(r.a, r.b, r.c, S.n);
+  if (p.cell) {
+    Cell c;
+    c.ok = r.w != CELL_BAD;
+    c.x = (int)(r.w & 1023u);
+    c.y = (int)((r.w >> 10) & 1023u);
+    c.z = (int)((r.w >> 20) & 1023u);
+    c.fx = r.a; c.fy = r.b; c.fz = r.c;
+    return c;
+  }
+  return cell_disp(S, r.w, r.a, r.b, r.c);
+}
+
 // xbits == 0 (resident batches): the key is the x-row number alone
 __device__ __forceinline__ unsigned cell_key(const Sim& S, const Cell& c) {
   const unsigned row = S.row_base + row_number(c.y, c.z, S.n);

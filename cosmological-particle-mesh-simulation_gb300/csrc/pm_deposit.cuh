@@ -66,12 +66,13 @@ __device__ __forceinline__ unsigned source_slot(const unsigned* __restrict__ per
   return perm ? __ldg(&perm[pos]) : pos;  // no permutation: the state is in row order
 }
 
-// Base cell of the source particle in `slot` relative to the tile; false if absent or bad.
+// Base cell of a source particle relative to the tile, from its loaded words; false if
+// absent or bad.
 template <int MODE>
-__device__ __forceinline__ bool slot_cell(const Sim& S, const Parts& p, unsigned slot, int y0, int z0, int* err,
-                                          Cell& c, int& ly, int& lz) {
-  if (slot == 0xffffffffu) return false;
-  c = particle_cell<MODE>(S, p, slot);
+__device__ __forceinline__ bool source_cell(const Sim& S, const Parts& p, const RawCell& raw, int y0, int z0,
+                                            int* err, Cell& c, int& ly, int& lz) {
+  if (!raw.present) return false;
+  c = raw_cell<MODE>(S, p, raw);
   const int n = S.n;
   int dy = c.y - y0, dz = c.z - z0;
   if (dy >= n - 1) dy -= n;
@@ -145,18 +146,18 @@ __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const
   __syncthreads();
   const unsigned total = s_off[NRUN];
   // two source entries per lane and iteration, so that their loads overlap; the slots (the
-  // permutation loads) of the next iteration are fetched before this one's cells
+  // permutation entries) of the next iteration are in flight while this one adds its particles
   unsigned base = (unsigned)warp * 32u;
   unsigned sl0 = source_slot(perm, s_begin, s_off, base + lane, total);
   unsigned sl1 = source_slot(perm, s_begin, s_off, base + NT + lane, total);
   for (; base < total; base += 2 * NT) {
-    const unsigned nb = base + 2 * NT;
-    const unsigned nx0 = source_slot(perm, s_begin, s_off, nb + lane, total);
-    const unsigned nx1 = source_slot(perm, s_begin, s_off, nb + NT + lane, total);
+    const RawCell q0 = load_raw_cell<MODE>(p, sl0), q1 = load_raw_cell<MODE>(p, sl1);
+    sl0 = source_slot(perm, s_begin, s_off, base + 2 * NT + lane, total);
+    sl1 = source_slot(perm, s_begin, s_off, base + 3 * NT + lane, total);
     Cell c0, c1;
     int ly0 = 0, lz0 = 0, ly1 = 0, lz1 = 0;
-    const bool ok0 = slot_cell<MODE>(S, p, sl0, y0, z0, err, c0, ly0, lz0);
-    const bool ok1 = slot_cell<MODE>(S, p, sl1, y0, z0, err, c1, ly1, lz1);
+    const bool ok0 = source_cell<MODE>(S, p, q0, y0, z0, err, c0, ly0, lz0);
+    const bool ok1 = source_cell<MODE>(S, p, q1, y0, z0, err, c1, ly1, lz1);
     if (ok0) {
       float wt[8];
       cic_weights(c0, wt);
@@ -167,8 +168,6 @@ __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const
       cic_weights(c1, wt);
       deposit_particle(lo, hi, n, rs, c1.x, ly1, lz1, wt);
     }
-    sl0 = nx0;
-    sl1 = nx1;
   }
   __syncthreads();
 }

@@ -281,10 +281,21 @@ __device__ __forceinline__ void fft_passes(float2* s, const float2* __restrict__
 // values per thread for it).
 __host__ __device__ constexpr bool blocked_pairs(int L) { return L % 3 != 0; }
 
+// Whether task j of a stride-1 pass over NP pairs of lines stores its R outputs in the order
+// r ^ 1: with 4 pairs, the 8 lanes of a quarter-warp (one phase of a 128-bit shared-memory
+// access) hold j and j + 1, whose outputs R j + r lie R 16-byte words apart -- a multiple
+// of the 8 words of a bank row, so in the same banks.  Odd j then write the neighbouring
+// word first, which sits 4 banks over: conflict-free phases.  The swap costs selects, so
+// only the shared-memory-bound z pass takes it (BANKS); the HBM-bound y passes do not.
+template <int NS, int NP>
+__device__ __forceinline__ bool store_swap(int j) {
+  return NS == 1 && NP == 4 && (j & 1);
+}
+
 // The same pass over pairs of adjacent lines of the Blocked layout (BW even): the two lines
 // share their element addresses' 16-byte words, so every shared-memory access is a
 // float4 (half the instructions) and every twiddle serves both lines.
-template <int L, int R, int NS, int NL, int BW, int NT, bool INV, class EPI = NoEpi>
+template <int L, int R, int NS, int NL, int BW, int NT, bool INV, class EPI = NoEpi, bool BANKS = false>
 __device__ __forceinline__ void stockham_pass_pairs(float2* s, const float2* __restrict__ tw, int tws,
                                                     const EPI& epi = EPI()) {
   static_assert(BW % 2 == 0 && NL % 2 == 0, "pairs of lines");
@@ -326,10 +337,14 @@ __device__ __forceinline__ void stockham_pass_pairs(float2* s, const float2* __r
       DFT<R, INV>::run(a[t]);
       DFT<R, INV>::run(b[t]);
       const int base = (j - k) * R + k;
+      // stride-1 stores of 4 pairs per j: the 8 lanes of a quarter-warp hold two j whose
+      // outputs fall in the same banks; odd j store in the order r ^ 1 (other banks)
+      const bool sw = BANKS && store_swap<NS, NP>(j);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const int e = base + r * NS;
-        const float2 x = epi(a[t][r], e, line), y = epi(b[t][r], e, line + 1);
+        const int e = base + (sw ? r ^ 1 : r) * NS;
+        const float2 av = sw ? a[t][r ^ 1] : a[t][r], bv = sw ? b[t][r ^ 1] : b[t][r];
+        const float2 x = epi(av, e, line), y = epi(bv, e, line + 1);
         s4[LAY::at(e, line) >> 1] = make_float4(x.x, x.y, y.x, y.y);
       }
     }
@@ -372,7 +387,7 @@ __device__ __forceinline__ void passes_span(float2* s, const float2* __restrict_
   if constexpr (P < PEND) {
     constexpr int R = plan_radix<L, P, REV>();
     if constexpr (blocked_pairs(L))
-      stockham_pass_pairs<L, R, NS, NL, BW, NT, INV>(s, tw, tws);
+      stockham_pass_pairs<L, R, NS, NL, BW, NT, INV, NoEpi, true>(s, tw, tws);
     else
       stockham_pass<L, R, NS, NL, Blocked<L, BW>, NT, INV>(s, tw, tws);
     passes_span<L, P + 1, PEND, NS * R, NL, BW, NT, INV, REV>(s, tw, tws);
@@ -432,12 +447,16 @@ __device__ __forceinline__ void stockham_turn(float2* s, const float2* __restric
       // inverse, first pass (stride 1: no twiddles), outputs j R + r
       DFT<R, true>::run(a[t]);
       if constexpr (PAIRS) DFT<R, true>::run(b[t]);
+      const bool sw = PAIRS && store_swap<1, NG>(j);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        if constexpr (PAIRS)
-          s4[LAY::at(j * R + r, line) >> 1] = make_float4(a[t][r].x, a[t][r].y, b[t][r].x, b[t][r].y);
-        else
+        const int rr = sw ? r ^ 1 : r;
+        if constexpr (PAIRS) {
+          const float2 av = sw ? a[t][r ^ 1] : a[t][r], bv = sw ? b[t][r ^ 1] : b[t][r];
+          s4[LAY::at(j * R + rr, line) >> 1] = make_float4(av.x, av.y, bv.x, bv.y);
+        } else {
           s[LAY::at(j * R + r, line)] = a[t][r];
+        }
       }
     }
   }
