@@ -571,8 +571,18 @@ __global__ void __launch_bounds__(xrow_nt(N)) k_x_row(const Sim* __restrict__ si
       xrow_untangle_store<N>(o, rb, t, tw, S.spec + row * S.pitch);
     } else {
       const float2* __restrict__ src = S.spec + row * S.pitch;
+      // all loads of the row issued before any store (the row is M + 1 values)
+      constexpr int NLD = (M + 1 + T - 1) / T;
+      float2 ld[NLD];
+#pragma unroll
+      for (int i = 0; i < NLD; ++i) {
+        const int k = t + T * i;
+        ld[i] = k <= M ? __ldg(&src[k]) : make_float2(0.f, 0.f);
+      }
       __syncwarp();
-      for (int k = t; k <= M; k += T) rb[k] = __ldg(&src[k]);
+#pragma unroll
+      for (int i = 0; i < NLD; ++i)
+        if (t + T * i <= M) rb[t + T * i] = ld[i];
       __syncwarp();
       // tangle: Z[j] = (X[j] + X*[M-j]) + i W^-j (X[j] - X*[M-j])
 #pragma unroll
