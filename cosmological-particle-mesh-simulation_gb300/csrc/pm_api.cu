@@ -11,6 +11,7 @@ struct pm_ctx {
   Tables tab;
   SortBufs sort;
   DBuf d_sim, d_prefix, d_err, d_maps;
+  DBuf tile_next;  // tile counter of the fused deposit
   const void* maps_for = nullptr;     // spectrum the device tensor maps describe
   DBuf row_start, spec, phi, rho;     // scratch grids
   DBuf hpos, hvel;                    // device copies for pm_step_host
@@ -241,6 +242,7 @@ int pm_ctx_create(const pm_config* cfg, int device, pm_ctx** out) {
   if (!e) e = c->d_sim.ensure(sizeof(Sim));
   if (!e) e = c->d_prefix.ensure(sizeof(int) * 2 * PH_COUNT);
   if (!e) e = c->d_err.ensure(sizeof(int));
+  if (!e) e = c->tile_next.ensure(sizeof(unsigned));
   if (!e) e = cudaMemset(c->d_err.p, 0, sizeof(int));
   if (!e) e = cudaDeviceSynchronize();
   if (e) {
@@ -258,6 +260,7 @@ void pm_ctx_destroy(pm_ctx* c) {
   c->d_sim.release();
   c->d_prefix.release();
   c->d_err.release();
+  c->tile_next.release();
   c->d_maps.release();
   c->row_start.release();
   c->spec.release();
@@ -439,7 +442,7 @@ int step_core(pm_ctx* c, const StepIO& io, long long np, double mass, double a, 
   if (!rho_out && deposit_r2c_supported(c->n)) {
     // the density is not requested: deposit straight into the x-transformed spectrum
     PM_CK(deposit_r2c_dispatch(c->n, c->d_sim.as<Sim>(), work(c, k, PH_DEP), sp, nullptr,
-                               c->row_start.as<unsigned>(), POS_ABS, c->d_err.as<int>(),
+                               c->row_start.as<unsigned>(), POS_ABS, c->d_err.as<int>(), c->tile_next.as<unsigned>(),
                                grid_for(k.prefix[PH_DEP][1], c->sms, deposit_r2c_ctas_per_sm(c->n)), st),
           "fused deposit");
     if (int r = spectral(c, k, false, st, true)) return r;

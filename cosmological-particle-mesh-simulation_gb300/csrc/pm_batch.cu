@@ -68,6 +68,7 @@ struct pm_batch {
   int cur = 0;
   SortBufs sort;
   DBuf row_start, d_sims, d_prefix, d_err, d_maps;
+  DBuf tile_next;  // tile counter of the fused deposit
   DBuf row_count, row_cursor, scan_sums;  // counting sort of the row keys
   Plan plan;
   bool dirty = true, keys_valid = false;
@@ -299,7 +300,8 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   for (size_t g = 0; g < P.sizes.size(); ++g) {
     PB_CK(spectral_dispatch(SPEC_PREPARE, P.sizes[g], nullptr, Work(), 0, st), "prepare");
     if (P.fused[g])
-      PB_CK(deposit_r2c_dispatch(P.sizes[g], nullptr, Work(), Parts(), nullptr, nullptr, POS_DISP, nullptr, 0, st),
+      PB_CK(deposit_r2c_dispatch(P.sizes[g], nullptr, Work(), Parts(), nullptr, nullptr, POS_DISP, nullptr, nullptr, 0,
+                                 st),
             "prepare fused deposit");
   }
   PB_CK(deposit_prepare(), "prepare deposit");
@@ -346,7 +348,7 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
     if (!P.fused[g]) continue;
     const int tot = P.fdep_total[g];
     PB_CK(deposit_r2c_dispatch(P.sizes[g], ds, work_of(b, PH_FIXED + 3 * (int)g + 2, tot), in, perm,
-                               b->row_start.as<unsigned>(), POS_DISP, err,
+                               b->row_start.as<unsigned>(), POS_DISP, err, b->tile_next.as<unsigned>(),
                                grid_for(tot, b->sms, deposit_r2c_ctas_per_sm(P.sizes[g])), st),
           "fused deposit");
   }
@@ -496,6 +498,7 @@ int pm_batch_create(int device, size_t mem_cap_bytes, pm_batch** out) {
   cudaError_t e = cudaSetDevice(device);
   if (!e) b->sms = sm_count(device);
   if (!e) e = b->d_err.ensure(sizeof(int));
+  if (!e) e = b->tile_next.ensure(sizeof(unsigned));
   if (!e) e = cudaMemset(b->d_err.p, 0, sizeof(int));
   if (!e) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
   if (!e) e = cudaDeviceSynchronize();
@@ -528,6 +531,7 @@ void pm_batch_destroy(pm_batch* b) {
   b->d_sims.release();
   b->d_prefix.release();
   b->d_err.release();
+  b->tile_next.release();
   b->d_maps.release();
   if (b->own) cudaStreamDestroy(b->own);
   delete b;

@@ -115,14 +115,17 @@ int spectral_ctas_per_sm(SpecKind kind, int n);
 cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int ctas, cudaStream_t st,
                               const CUtensorMap* maps = nullptr, int* err = nullptr);
 cudaError_t launch_fourier_grid(const Sim* sims, int ctas, cudaStream_t st);
-// fused deposit + x R2C (the density grid is not written); ctas <= 0 only prepares
+// fused deposit + x R2C (the density grid is not written); ctas <= 0 only prepares.
+// next_tile: one device word, the tile counter (zeroed on `st` before the launch); nullptr:
+// CTAs take every ctas-th tile.
 template <int N>
 cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned* perm, const unsigned* row_start,
-                               int mode, int* err, int ctas, cudaStream_t st);
+                               int mode, int* err, unsigned* next_tile, int ctas, cudaStream_t st);
 bool deposit_r2c_supported(int n);
 int deposit_r2c_ctas_per_sm(int n);  // resident CTAs per SM of the fused deposit
 cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const unsigned* perm,
-                                 const unsigned* row_start, int mode, int* err, int ctas, cudaStream_t st);
+                                 const unsigned* row_start, int mode, int* err, unsigned* next_tile, int ctas,
+                                 cudaStream_t st);
 
 // sum of the first n_slices planes of an n^3 grid, float64 n^2 output (pm_diagnostics.cu)
 cudaError_t launch_project(const float* rho, int n, int n_slices, double* out, int ctas, cudaStream_t st);

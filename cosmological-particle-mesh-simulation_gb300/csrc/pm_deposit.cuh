@@ -28,12 +28,12 @@ __device__ __forceinline__ float fixed_to_float(unsigned l, unsigned c, float sc
   return __ull2float_rn(est + (unsigned)(l - (unsigned)est)) * scale;
 }
 
-// Adds the 8 weights of a particle with base cell (cx, ly, lz) (ly, lz relative to the
-// tile, in [-1, TY-1] x [-1, TZ-1]) to the tile accumulators; tile row r of lo / hi starts
-// at word r * rs.  Corners outside the tile's rows are skipped (a neighbouring tile adds
-// them), unless the whole particle is inside.
+// Adds the 8 quantised weights q of a particle with base cell (cx, ly, lz) (ly, lz relative
+// to the tile, in [-1, TY-1] x [-1, TZ-1]) to the tile accumulators; tile row r of lo / hi
+// starts at word r * rs.  Corners outside the tile's rows are skipped (a neighbouring tile
+// adds them), unless the whole particle is inside.
 __device__ __forceinline__ void deposit_particle(unsigned* lo, unsigned* hi, int n, int rs, int cx, int ly, int lz,
-                                                 const float (&wt)[8]) {
+                                                 const unsigned (&q)[8]) {
   const int x1 = cx + 1 == n ? 0 : cx + 1;
   const bool inside = (unsigned)ly < (unsigned)(TY - 1) && (unsigned)lz < (unsigned)(TZ - 1);
   const int base = (lz * TY + ly) * rs;
@@ -41,8 +41,27 @@ __device__ __forceinline__ void deposit_particle(unsigned* lo, unsigned* hi, int
   for (int k = 0; k < 8; ++k) {
     const int ty2 = ly + corner_y(k), tz2 = lz + corner_z(k);
     if (inside || (ty2 >= 0 && ty2 < TY && tz2 >= 0 && tz2 < TZ))
-      acc_add(lo, hi, base + (corner_z(k) * TY + corner_y(k)) * rs + (corner_x(k) ? x1 : cx),
-              __float2uint_rn(wt[k] * (float)(1u << PM_FIX_BITS)));
+      acc_add(lo, hi, base + (corner_z(k) * TY + corner_y(k)) * rs + (corner_x(k) ? x1 : cx), q[k]);
+  }
+}
+
+// Quantised CIC weights (2^-26) of a particle.
+__device__ __forceinline__ void quantised_weights(const Cell& c, unsigned (&q)[8]) {
+  float wt[8];
+  cic_weights(c, wt);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) q[k] = __float2uint_rn(wt[k] * (float)(1u << PM_FIX_BITS));
+}
+
+// (Pre-adding the weights of lanes that share a cell, with __match_any_sync and a warp
+// reduction, would cut the same-address atomics of clustered tiles, but the match alone made
+// the deposit 6x slower on GB300.)
+__device__ __forceinline__ void deposit_entry(unsigned* lo, unsigned* hi, int n, int rs, bool ok, const Cell& c,
+                                              int ly, int lz) {
+  if (ok) {
+    unsigned q[8];
+    quantised_weights(c, q);
+    deposit_particle(lo, hi, n, rs, c.x, ly, lz, q);
   }
 }
 
@@ -158,16 +177,8 @@ __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const
     int ly0 = 0, lz0 = 0, ly1 = 0, lz1 = 0;
     const bool ok0 = source_cell<MODE>(S, p, q0, y0, z0, err, c0, ly0, lz0);
     const bool ok1 = source_cell<MODE>(S, p, q1, y0, z0, err, c1, ly1, lz1);
-    if (ok0) {
-      float wt[8];
-      cic_weights(c0, wt);
-      deposit_particle(lo, hi, n, rs, c0.x, ly0, lz0, wt);
-    }
-    if (ok1) {
-      float wt[8];
-      cic_weights(c1, wt);
-      deposit_particle(lo, hi, n, rs, c1.x, ly1, lz1, wt);
-    }
+    deposit_entry(lo, hi, n, rs, ok0, c0, ly0, lz0);
+    deposit_entry(lo, hi, n, rs, ok1, c1, ly1, lz1);
   }
   __syncthreads();
 }

@@ -767,7 +767,7 @@ __host__ __device__ constexpr bool deposit_r2c_ok(int n) { return (TZ * TY * n) 
 template <int N, int MODE>
 __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
     k_deposit_r2c(const Sim* __restrict__ sims, Work w, Parts p, const unsigned* __restrict__ perm,
-                  const unsigned* __restrict__ row_start, int* err) {
+                  const unsigned* __restrict__ row_start, int* err, unsigned* __restrict__ next_tile) {
   constexpr int NT = deposit_r2c_nt(N);
   constexpr int M = N / 2, NL = TZ * TY, LS = NL + 1;
   constexpr int PER = NL * N / NT;
@@ -783,7 +783,14 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
   float2* F = reinterpret_cast<float2*>(acc_raw);
   float* Ff = reinterpret_cast<float*>(acc_raw);
   bool runs_ready = false;  // the run table of this tile was loaded during the previous one
-  for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
+  // Tiles are taken from a counter (zero at launch) after the first, one per CTA: a tile's
+  // work is its particle count, which clustering makes very uneven, so a fixed stride
+  // leaves the CTAs that drew the dense tiles running alone at the end.
+  __shared__ int s_next;
+  auto take_next = [&](int unit) -> int {
+    return next_tile ? (int)gridDim.x + (int)atomicAdd(next_tile, 1u) : unit + (int)gridDim.x;
+  };
+  for (int unit = blockIdx.x; unit < w.total;) {
     const int si = locate_sim(w, unit);
     const Sim& S = sims[si];
     const int local = unit - __ldg(&w.prefix[si]);
@@ -813,10 +820,11 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
             const uint2 ll = l2[j], hh = h2[j];
             v2[i][a] = make_float2(fixed_to_float(ll.x, hh.x, ms), fixed_to_float(ll.y, hh.y, ms));
           }
-        // warp 0 loads the next tile's run table now and stores it after the transform,
-        // so that the loads' latency hides behind it (the table is free: the particle loop
-        // of this tile is over)
-        const int next = unit + gridDim.x;
+        // warp 0 takes the next tile and loads its run table now, and stores it after the
+        // transform, so that the loads' latency hides behind it (the table is free: the
+        // particle loop of this tile is over)
+        int next = 0;
+        if (threadIdx.x < 32) next = __shfl_sync(FULL, lane == 0 ? take_next(unit) : 0, 0);
         RunLoad nl{0u, 0u};
         int nsi = 0, ny0 = 0, nz0 = 0;
         if (threadIdx.x < 32 && next < w.total) {
@@ -830,9 +838,11 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
         const long long row = (long long)(z0 + r / TY) * N + (y0 + r % TY);
         xrow_untangle_store<N>(o2, rb, t, S.tw, S.spec + row * S.pitch);
         if (threadIdx.x < 32 && next < w.total) run_table(nl, lane, s_begin, s_off);
+        if (threadIdx.x == 0) s_next = next;
       }
       __syncthreads();
       runs_ready = true;
+      unit = s_next;
       continue;
     }
     float v[PER];
@@ -861,13 +871,15 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
       const float2 o = cscale(mul_mi<false>(csub(zk, zc)), 0.5f);
       dst[row * P + k] = cadd(e, cmul(__ldg(&S.tw[k]), o));
     }
+    if (threadIdx.x == 0) s_next = take_next(unit);
     __syncthreads();
+    unit = s_next;
   }
 }
 
 template <int N>
 cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned* perm, const unsigned* row_start,
-                               int mode, int* err, int ctas, cudaStream_t st) {
+                               int mode, int* err, unsigned* next_tile, int ctas, cudaStream_t st) {
   if constexpr (!deposit_r2c_ok(N)) {
     return cudaErrorNotSupported;
   } else {
@@ -883,8 +895,12 @@ cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned*
   }
   if (ctas <= 0) return cudaSuccess;  // attribute setup only
   constexpr int NT = deposit_r2c_nt(N);
-  if (mode == POS_ABS) k_deposit_r2c<N, POS_ABS><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err);
-  else k_deposit_r2c<N, POS_DISP><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err);
+  if (next_tile) {
+    const cudaError_t e = cudaMemsetAsync(next_tile, 0, sizeof(unsigned), st);
+    if (e) return e;
+  }
+  if (mode == POS_ABS) k_deposit_r2c<N, POS_ABS><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err, next_tile);
+  else k_deposit_r2c<N, POS_DISP><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err, next_tile);
   return cudaGetLastError();
   }
 }
