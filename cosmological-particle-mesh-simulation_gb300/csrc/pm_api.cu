@@ -443,7 +443,7 @@ int step_core(pm_ctx* c, const StepIO& io, long long np, double mass, double a, 
     // the density is not requested: deposit straight into the x-transformed spectrum
     PM_CK(deposit_r2c_dispatch(c->n, c->d_sim.as<Sim>(), work(c, k, PH_DEP), sp, nullptr,
                                c->row_start.as<unsigned>(), POS_ABS, c->d_err.as<int>(), c->tile_next.as<unsigned>(),
-                               grid_for(k.prefix[PH_DEP][1], c->sms, deposit_r2c_ctas_per_sm(c->n)), st),
+                               nullptr, grid_for(k.prefix[PH_DEP][1], c->sms, deposit_r2c_ctas_per_sm(c->n)), st),
           "fused deposit");
     if (int r = spectral(c, k, false, st, true)) return r;
   } else {

@@ -68,7 +68,8 @@ struct pm_batch {
   int cur = 0;
   SortBufs sort;
   DBuf row_start, d_sims, d_prefix, d_err, d_maps;
-  DBuf tile_next;  // tile counter of the fused deposit
+  DBuf tile_next;   // tile counter of the fused deposit, and 2 words of scratch for the ordering
+  DBuf tile_order;  // the fused deposit's tiles, dense first
   DBuf row_count, row_cursor, scan_sums;  // counting sort of the row keys
   Plan plan;
   bool dirty = true, keys_valid = false;
@@ -290,6 +291,11 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   PB_CK(b->d_prefix.ensure(sizeof(int) * pre.size()), "alloc prefix");
   PB_CK(b->row_start.ensure(sizeof(unsigned) * ((size_t)rows + 1)), "alloc rows");
   PB_CK(b->row_count.ensure(sizeof(unsigned) * (size_t)rows), "alloc rows");
+  {
+    size_t tiles = 1;
+    for (int t : P.fdep_total) tiles = std::max(tiles, (size_t)t);
+    PB_CK(b->tile_order.ensure(sizeof(unsigned) * tiles), "alloc tile order");
+  }
   PB_CK(b->row_cursor.ensure(sizeof(unsigned) * (size_t)rows), "alloc rows");
   PB_CK(b->scan_sums.ensure(sizeof(unsigned) * row_sort_block_sums(rows)), "alloc rows");
   PB_CK(cudaMemcpyAsync(b->d_sims.p, hs.data(), sizeof(Sim) * S, cudaMemcpyHostToDevice, st), "upload sims");
@@ -300,8 +306,8 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   for (size_t g = 0; g < P.sizes.size(); ++g) {
     PB_CK(spectral_dispatch(SPEC_PREPARE, P.sizes[g], nullptr, Work(), 0, st), "prepare");
     if (P.fused[g])
-      PB_CK(deposit_r2c_dispatch(P.sizes[g], nullptr, Work(), Parts(), nullptr, nullptr, POS_DISP, nullptr, nullptr, 0,
-                                 st),
+      PB_CK(deposit_r2c_dispatch(P.sizes[g], nullptr, Work(), Parts(), nullptr, nullptr, POS_DISP, nullptr, nullptr,
+                                 nullptr, 0, st),
             "prepare fused deposit");
   }
   PB_CK(deposit_prepare(), "prepare deposit");
@@ -347,8 +353,12 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
   for (size_t g = 0; g < P.sizes.size(); ++g) {
     if (!P.fused[g]) continue;
     const int tot = P.fdep_total[g];
-    PB_CK(deposit_r2c_dispatch(P.sizes[g], ds, work_of(b, PH_FIXED + 3 * (int)g + 2, tot), in, perm,
-                               b->row_start.as<unsigned>(), POS_DISP, err, b->tile_next.as<unsigned>(),
+    const Work wg = work_of(b, PH_FIXED + 3 * (int)g + 2, tot);
+    PB_CK(launch_tile_order(ds, wg, b->row_start.as<unsigned>(), b->tile_order.as<unsigned>(),
+                            b->tile_next.as<unsigned>() + 2, b->sms, st),
+          "tile order");
+    PB_CK(deposit_r2c_dispatch(P.sizes[g], ds, wg, in, perm, b->row_start.as<unsigned>(), POS_DISP, err,
+                               b->tile_next.as<unsigned>(), b->tile_order.as<unsigned>(),
                                grid_for(tot, b->sms, deposit_r2c_ctas_per_sm(P.sizes[g])), st),
           "fused deposit");
   }
@@ -384,7 +394,9 @@ int launches_per_step(pm_batch* b) {
   // counting sort: 3 scan kernels and the scatter (the kick makes the histogram; the count
   // reset is a memset)
   int n = 4 + (P.fixed_total[PH_DEP] > 0 ? 1 : 0) + 5 * (int)P.sizes.size() + 1 + 1;
-  return n;  // each fused size replaces its x R2C launch by the fused deposit
+  // each fused size replaces its x R2C launch by the fused deposit, preceded by its tile order
+  for (int f : P.fused) n += f;
+  return n;
 }
 
 int ensure_keys(pm_batch* b, cudaStream_t st) {
@@ -498,7 +510,7 @@ int pm_batch_create(int device, size_t mem_cap_bytes, pm_batch** out) {
   cudaError_t e = cudaSetDevice(device);
   if (!e) b->sms = sm_count(device);
   if (!e) e = b->d_err.ensure(sizeof(int));
-  if (!e) e = b->tile_next.ensure(sizeof(unsigned));
+  if (!e) e = b->tile_next.ensure(4 * sizeof(unsigned));
   if (!e) e = cudaMemset(b->d_err.p, 0, sizeof(int));
   if (!e) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
   if (!e) e = cudaDeviceSynchronize();
@@ -532,6 +544,7 @@ void pm_batch_destroy(pm_batch* b) {
   b->d_prefix.release();
   b->d_err.release();
   b->tile_next.release();
+  b->tile_order.release();
   b->d_maps.release();
   if (b->own) cudaStreamDestroy(b->own);
   delete b;

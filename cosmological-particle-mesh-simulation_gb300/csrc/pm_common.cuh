@@ -117,15 +117,17 @@ cudaError_t spectral_dispatch(SpecKind kind, int n, const Sim* sims, Work w, int
 cudaError_t launch_fourier_grid(const Sim* sims, int ctas, cudaStream_t st);
 // fused deposit + x R2C (the density grid is not written); ctas <= 0 only prepares.
 // next_tile: one device word, the tile counter (zeroed on `st` before the launch); nullptr:
-// CTAs take every ctas-th tile.
+// CTAs take every ctas-th tile.  order (optional, w.total entries): the tiles in the order to
+// take them (launch_tile_order).
 template <int N>
 cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned* perm, const unsigned* row_start,
-                               int mode, int* err, unsigned* next_tile, int ctas, cudaStream_t st);
+                               int mode, int* err, unsigned* next_tile, const unsigned* order, int ctas,
+                               cudaStream_t st);
 bool deposit_r2c_supported(int n);
 int deposit_r2c_ctas_per_sm(int n);  // resident CTAs per SM of the fused deposit
 cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const unsigned* perm,
-                                 const unsigned* row_start, int mode, int* err, unsigned* next_tile, int ctas,
-                                 cudaStream_t st);
+                                 const unsigned* row_start, int mode, int* err, unsigned* next_tile,
+                                 const unsigned* order, int ctas, cudaStream_t st);
 
 // sum of the first n_slices planes of an n^3 grid, float64 n^2 output (pm_diagnostics.cu)
 cudaError_t launch_project(const float* rho, int n, int n_slices, double* out, int ctas, cudaStream_t st);
@@ -157,6 +159,9 @@ cudaError_t launch_coef(Sim* sims, int nsims, int advance, cudaStream_t st);
 cudaError_t launch_gather_state(const float* pos, const float* vel, long long np, const unsigned* idx, float* spos,
                                 float* svel, int sms, cudaStream_t st);
 cudaError_t deposit_prepare();  // sets kernel attributes (call before graph capture)
+// order of the fused deposit's tiles (dense tiles first); counts: 2 device words of scratch
+cudaError_t launch_tile_order(const Sim* sims, const Work& w, const unsigned* row_start, unsigned* order,
+                              unsigned* counts, int sms, cudaStream_t st);
 cudaError_t launch_abs_to_disp(const float* pos, const float* vel, long long np, int np1, int n,
                                const int* q_int, const float* q_frac, Parts out, long long off,
                                cudaStream_t st);

@@ -413,6 +413,39 @@ cudaError_t launch_row_start(const unsigned* keys, long long n, int xbits, unsig
   return cudaGetLastError();
 }
 
+// Order in which the fused deposit takes its tiles: the dense tiles first.  A tile's work is
+// its source-entry count, which clustering makes very uneven; a dense tile taken late runs on
+// alone after the others have finished.  Tiles with more than twice the mean count go to the
+// front of `order`, the others to the back (their order within each part is immaterial: a
+// tile's sums do not depend on when it runs).  counts[0], counts[1]: zero at launch.
+__global__ void k_tile_order(const Sim* __restrict__ sims, Work w, const unsigned* __restrict__ row_start,
+                             unsigned* __restrict__ order, unsigned* __restrict__ counts) {
+  for (int unit = blockIdx.x * blockDim.x + threadIdx.x; unit < w.total; unit += gridDim.x * blockDim.x) {
+    const int si = locate_sim(w, unit);
+    const Sim& S = sims[si];
+    const int n = S.n, local = unit - __ldg(&w.prefix[si]);
+    const int y0 = (local % (n / TY)) * TY, z0 = (local / (n / TY)) * TZ;
+    unsigned cnt = 0;
+#pragma unroll
+    for (int r = 0; r < NRUN; ++r) cnt += run_load(S, row_start, y0, z0, r).cnt;
+    // mean source entries per tile: each particle once, plus its tile's last plane / row / corner
+    const double ntiles = (double)(n / TY) * (n / TZ);
+    const double mean = (double)S.np * (1.0 + 1.0 / TZ + 1.0 / TY + 1.0 / (TY * TZ)) / ntiles;
+    if (cnt > 2.0 * mean) order[atomicAdd(&counts[0], 1u)] = (unsigned)unit;
+    else order[w.total - 1 - (int)atomicAdd(&counts[1], 1u)] = (unsigned)unit;
+  }
+}
+
+cudaError_t launch_tile_order(const Sim* sims, const Work& w, const unsigned* row_start, unsigned* order,
+                              unsigned* counts, int sms, cudaStream_t st) {
+  if (w.total <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned), st);
+  if (e) return e;
+  const int ctas = std::min((w.total + 255) / 256, 4 * sms);
+  k_tile_order<<<ctas, 256, 0, st>>>(sims, w, row_start, order, counts);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_deposit(const Sim* sims, const Work& w, Parts p, const unsigned* perm,
                            const unsigned* row_start, int mode, int* err, int ctas, size_t smem,
                            cudaStream_t st) {

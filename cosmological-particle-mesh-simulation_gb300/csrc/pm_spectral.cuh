@@ -767,7 +767,8 @@ __host__ __device__ constexpr bool deposit_r2c_ok(int n) { return (TZ * TY * n) 
 template <int N, int MODE>
 __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
     k_deposit_r2c(const Sim* __restrict__ sims, Work w, Parts p, const unsigned* __restrict__ perm,
-                  const unsigned* __restrict__ row_start, int* err, unsigned* __restrict__ next_tile) {
+                  const unsigned* __restrict__ row_start, int* err, unsigned* __restrict__ next_tile,
+                  const unsigned* __restrict__ order) {
   constexpr int NT = deposit_r2c_nt(N);
   constexpr int M = N / 2, NL = TZ * TY, LS = NL + 1;
   constexpr int PER = NL * N / NT;
@@ -786,11 +787,14 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
   // Tiles are taken from a counter (zero at launch) after the first, one per CTA: a tile's
   // work is its particle count, which clustering makes very uneven, so a fixed stride
   // leaves the CTAs that drew the dense tiles running alone at the end.
+  // `order` (optional) lists the tiles dense-first; idx is the place in it.
   __shared__ int s_next;
-  auto take_next = [&](int unit) -> int {
-    return next_tile ? (int)gridDim.x + (int)atomicAdd(next_tile, 1u) : unit + (int)gridDim.x;
+  auto take_next = [&](int idx) -> int {
+    return next_tile ? (int)gridDim.x + (int)atomicAdd(next_tile, 1u) : idx + (int)gridDim.x;
   };
-  for (int unit = blockIdx.x; unit < w.total;) {
+  auto tile_at = [&](int idx) -> int { return order ? (int)__ldg(&order[idx]) : idx; };
+  for (int idx = blockIdx.x; idx < w.total;) {
+    const int unit = tile_at(idx);
     const int si = locate_sim(w, unit);
     const Sim& S = sims[si];
     const int local = unit - __ldg(&w.prefix[si]);
@@ -824,12 +828,13 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
         // transform, so that the loads' latency hides behind it (the table is free: the
         // particle loop of this tile is over)
         int next = 0;
-        if (threadIdx.x < 32) next = __shfl_sync(FULL, lane == 0 ? take_next(unit) : 0, 0);
+        if (threadIdx.x < 32) next = __shfl_sync(FULL, lane == 0 ? take_next(idx) : 0, 0);
         RunLoad nl{0u, 0u};
         int nsi = 0, ny0 = 0, nz0 = 0;
         if (threadIdx.x < 32 && next < w.total) {
-          nsi = locate_sim(w, next);
-          const int nloc = next - __ldg(&w.prefix[nsi]);
+          const int nunit = tile_at(next);
+          nsi = locate_sim(w, nunit);
+          const int nloc = nunit - __ldg(&w.prefix[nsi]);
           ny0 = (nloc % (N / TY)) * TY;
           nz0 = (nloc / (N / TY)) * TZ;
           nl = run_load(sims[nsi], row_start, ny0, nz0, lane);
@@ -842,7 +847,7 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
       }
       __syncthreads();
       runs_ready = true;
-      unit = s_next;
+      idx = s_next;
       continue;
     }
     float v[PER];
@@ -871,15 +876,16 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
       const float2 o = cscale(mul_mi<false>(csub(zk, zc)), 0.5f);
       dst[row * P + k] = cadd(e, cmul(__ldg(&S.tw[k]), o));
     }
-    if (threadIdx.x == 0) s_next = take_next(unit);
+    if (threadIdx.x == 0) s_next = take_next(idx);
     __syncthreads();
-    unit = s_next;
+    idx = s_next;
   }
 }
 
 template <int N>
 cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned* perm, const unsigned* row_start,
-                               int mode, int* err, unsigned* next_tile, int ctas, cudaStream_t st) {
+                               int mode, int* err, unsigned* next_tile, const unsigned* order, int ctas,
+                               cudaStream_t st) {
   if constexpr (!deposit_r2c_ok(N)) {
     return cudaErrorNotSupported;
   } else {
@@ -899,8 +905,10 @@ cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned*
     const cudaError_t e = cudaMemsetAsync(next_tile, 0, sizeof(unsigned), st);
     if (e) return e;
   }
-  if (mode == POS_ABS) k_deposit_r2c<N, POS_ABS><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err, next_tile);
-  else k_deposit_r2c<N, POS_DISP><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err, next_tile);
+  if (mode == POS_ABS)
+    k_deposit_r2c<N, POS_ABS><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err, next_tile, order);
+  else
+    k_deposit_r2c<N, POS_DISP><<<ctas, NT, sm, st>>>(sims, w, p, perm, row_start, err, next_tile, order);
   return cudaGetLastError();
   }
 }

@@ -11,16 +11,16 @@ PM_FOR_EACH_N(PM_EXTERN)
 #undef PM_EXTERN
 #define PM_EXTERN(NN)                                                                                         \
   extern template cudaError_t deposit_r2c_launch<NN>(const Sim*, Work, Parts, const unsigned*, const unsigned*, \
-                                                     int, int*, unsigned*, int, cudaStream_t);
+                                                     int, int*, unsigned*, const unsigned*, int, cudaStream_t);
 PM_FOR_EACH_N(PM_EXTERN)
 #undef PM_EXTERN
 
 cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const unsigned* perm,
-                                 const unsigned* row_start, int mode, int* err, unsigned* next_tile, int ctas,
-                                 cudaStream_t st) {
+                                 const unsigned* row_start, int mode, int* err, unsigned* next_tile,
+                                 const unsigned* order, int ctas, cudaStream_t st) {
   switch (n) {
 #define PM_CASE(NN) \
-  case NN: return deposit_r2c_launch<NN>(sims, w, p, perm, row_start, mode, err, next_tile, ctas, st);
+  case NN: return deposit_r2c_launch<NN>(sims, w, p, perm, row_start, mode, err, next_tile, order, ctas, st);
     PM_FOR_EACH_N(PM_CASE)
 #undef PM_CASE
     default: return cudaErrorInvalidValue;

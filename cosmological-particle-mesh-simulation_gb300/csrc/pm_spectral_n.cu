@@ -8,5 +8,5 @@
 namespace pm {
 template cudaError_t spectral_launch<PM_N>(SpecKind, const Sim*, Work, int, cudaStream_t, const CUtensorMap*, int*);
 template cudaError_t deposit_r2c_launch<PM_N>(const Sim*, Work, Parts, const unsigned*, const unsigned*, int, int*,
-                                              unsigned*, int, cudaStream_t);
+                                              unsigned*, const unsigned*, int, cudaStream_t);
 }
