@@ -192,3 +192,73 @@ def test_snapshot_units_and_file_roundtrip(tmp_path):
     write_file(path, d)
     back = read_file(path)
     assert set(back) == set(d) and all(np.array_equal(back[k], d[k]) for k in d)
+
+
+# ---- index algebra of the shared-memory transforms (pm_fft.cuh), restated in numpy ----------
+def _fft_plans():
+    """The radix plans as pm_fft.cuh declares them (PM_PLAN(L, r0, r1, ...))."""
+    src = open(os.path.join(ROOT, "cosmological-particle-mesh-simulation_gb300", "csrc", "pm_fft.cuh")).read()
+    plans = {}
+    for m in re.finditer(r"^PM_PLAN\((\d+),\s*([\d,\s]+)\)", src, re.M):
+        plans[int(m.group(1))] = [int(x) for x in m.group(2).split(",")]
+    return plans
+
+
+def _stockham_pass(x, L, R, NS, inv, swap=False):
+    """One pass as stockham_pass / stockham_pass_pairs index it: task j loads x[j + r L/R],
+    twiddles by w^(r k L/(NS R)) (k = j mod NS), a radix-R DFT, stores at (j - k) R + k + r NS;
+    with `swap` (stride-1 passes of 4-pair bundles) odd j store output r ^ 1 at step r."""
+    NB = L // R
+    y = np.empty_like(x)
+    sgn = 1 if inv else -1
+    dft = np.exp(sgn * 2j * np.pi * np.outer(np.arange(R), np.arange(R)) / R)
+    for j in range(NB):
+        k = j % NS
+        v = x[j + NB * np.arange(R)].copy()
+        if NS > 1:
+            v[1:] *= np.exp(sgn * 2j * np.pi * (np.arange(1, R) * k * (L // (NS * R))) / L)
+        out = dft @ v
+        base = (j - k) * R + k
+        for r in range(R):
+            rr = r ^ 1 if (swap and NS == 1 and (j & 1)) else r
+            y[base + rr * NS] = out[rr]
+    return y
+
+
+@pytest.mark.parametrize("L", sorted(_fft_plans()))
+def test_stockham_plans_and_z_turn(L):
+    """Each plan is a DFT; the z pass's turn (last forward pass, the Green multiply and the
+    first pass of an inverse run on the reversed plan, all on one thread's registers) equals
+    ifft(fft(x) g) L; the pair-swapped store order changes nothing but the order."""
+    plan = _fft_plans()[L]
+    assert int(np.prod(plan)) == L
+    pairs = L % 3 != 0  # blocked_pairs(L): the pair passes, which may swap their store order
+    rng = np.random.default_rng(L)
+    x = rng.standard_normal(L) + 1j * rng.standard_normal(L)
+    g = rng.standard_normal(L)
+    y, NS = x, 1
+    for R in plan:
+        y = _stockham_pass(y, L, R, NS, False, swap=pairs)
+        NS *= R
+    assert np.allclose(y, np.fft.fft(x), atol=1e-9 * L)
+    # the turn
+    y, NS = x, 1
+    for R in plan[:-1]:
+        y = _stockham_pass(y, L, R, NS, False, swap=pairs)
+        NS *= R
+    R = plan[-1]
+    NSL = L // R
+    t = np.empty_like(y)
+    for j in range(NSL):
+        v = y[j + NSL * np.arange(R)].copy()
+        if NSL > 1:
+            v[1:] *= np.exp(-2j * np.pi * np.arange(1, R) * j / L)
+        v = np.exp(-2j * np.pi * np.outer(np.arange(R), np.arange(R)) / R) @ v  # forward, last pass
+        v *= g[j + NSL * np.arange(R)]                                            # the Green multiply
+        v = np.exp(2j * np.pi * np.outer(np.arange(R), np.arange(R)) / R) @ v     # inverse, first pass
+        t[j * R + np.arange(R)] = v
+    y, NS = t, R
+    for R2 in plan[-2::-1]:
+        y = _stockham_pass(y, L, R2, NS, True, swap=pairs)
+        NS *= R2
+    assert np.allclose(y, np.fft.ifft(np.fft.fft(x) * g) * L, atol=1e-9 * L)
