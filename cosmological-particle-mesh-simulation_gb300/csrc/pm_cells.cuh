@@ -27,7 +27,7 @@ __device__ __forceinline__ unsigned row_number(int y, int z, int n) {
   return tile * (unsigned)(TZ * TY) + (unsigned)((z % TZ) * TY + (y % TY));
 }
 
-// Q4: a float32 coordinate equal to n (or slightly negative) is mapped into [0, n).
+// A float32 coordinate equal to n (or slightly negative) is mapped into [0, n).
 __device__ __forceinline__ float canon(float x, float fn) {
   if (x >= fn) x -= fn;
   if (x < 0.f) x += fn;

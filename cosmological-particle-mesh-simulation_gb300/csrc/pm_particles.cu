@@ -202,7 +202,7 @@ __device__ __forceinline__ unsigned kick_store(const Sim& S, const Parts& out, l
   vy = fmaf(kk, g[1], vy);
   vz = fmaf(kk, g[2], vz);
   if (MODE == POS_ABS) {
-    // positions may arrive as exactly n (Q4): drift the canonical value and wrap
+    // positions may arrive as exactly n: drift the canonical value and wrap
     const float fn = (float)S.n;
     const float nx = canon(fmaf(dr, vx, canon(px, fn)), fn);
     const float ny = canon(fmaf(dr, vy, canon(py, fn)), fn);

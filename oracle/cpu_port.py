@@ -1,6 +1,6 @@
 """Multi-threaded CPU port of the reference step, the CPU baseline of bench.py.
 
-TEST INFRASTRUCTURE ONLY (the checker's CPU arm): the particle loops run in
+TEST INFRASTRUCTURE ONLY (part of the oracle): the particle loops run in
 oracle/cpu_step.c (C + OpenMP, float64 arithmetic, float32 state as in the reference), the
 FFT Poisson solve in scipy.fft with the same number of threads (oracle/pm_oracle.potential;
 the reference threads pyFFTW with N_CPU).  Checked against oracle/pm_oracle.py by

@@ -1,7 +1,7 @@
 /*
  * Multi-threaded CPU restatement of the reference's particle loops, for the CPU baseline.
  *
- * TEST INFRASTRUCTURE ONLY (the checker's CPU arm): called by bench.py's cpu_baseline /
+ * TEST INFRASTRUCTURE ONLY (part of the oracle): called by bench.py's cpu_baseline /
  * --impl reference leg and by the tests that check it against oracle/pm_oracle.py; the
  * product never links it.  It restates, in float64 with OpenMP threads over particles (the
  * reference parallelises the same loops with numba prange over N_CPU threads):
@@ -17,7 +17,7 @@
  * Positions and velocities are float32 (3, np) arrays as in the reference; the potential
  * is float64 (the reference's complex128 FFT output, real part).  The FFT step between
  * them (potential.py) runs in scipy.fft with the same threads.  Positions are first mapped
- * into [0, n) (the engine's decision for the x == n case, oracle Q4).
+ * into [0, n) (the engine's decision for the x == n case, quirk Q4 of oracle/pm_oracle.py).
  */
 #include <math.h>
 #include <stddef.h>

@@ -1,6 +1,6 @@
 """FP64 CPU oracle for the particle-mesh hot path.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker: only ``tests/``,
+TEST INFRASTRUCTURE ONLY.  This module is the oracle: only ``tests/``,
 ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference`` leg of
 ``bench.py`` may import it.  The product path (the CUDA library and its Python
 host layer) never calls into it.

@@ -1,6 +1,6 @@
 """FP64 torch copy of the oracle's PM step, for full-size checks on a GPU.
 
-TEST INFRASTRUCTURE ONLY (the checker): used by tests/ to run the reference algorithm in
+TEST INFRASTRUCTURE ONLY (part of the oracle): used by tests/ to run the reference algorithm in
 float64 at sizes the numpy oracle cannot reach (512^3 grids, 1000 steps).  It follows
 oracle/pm_oracle.py function for function -- density (density.py:7-48), potential
 (potential.py:7-29, FFTs in complex128), integrate (integrate.py:15-97) and the step

@@ -1,6 +1,6 @@
 """Parity of the CUDA hot path (through the C ABI) with the reference and the FP64 oracle.
 
-Tolerances (the benchmark spec): cell keys, sorted keys and permutation bit-exact; density
+Tolerances: cell keys, sorted keys and permutation bit-exact; density
 and potential within 1e-5 relative L2 of the FP64 oracle; total mass exact to float32
 rounding.  Kick/drift: velocities within 1e-5 relative L2, positions within a few
 float32 ulps of the grid size.
@@ -164,7 +164,7 @@ def test_uniform_lattice_and_edges(cuda):
     pos = np.stack([x.ravel(), y.ravel(), z.ravel()])
     rho = ctx.density(dev(torch, pos), 1.0).cpu().numpy()
     assert np.array_equal(rho, np.ones_like(rho))
-    # Q4 edge: x == N exactly, x = N - eps, x = 0 (periodic wrap of the CIC corners)
+    # edge (oracle quirk Q4): x == N exactly, x = N - eps, x = 0 (periodic wrap of the CIC corners)
     edge = np.array([[n, n - 1e-4, 0.0, 31.999998], [0.5, 5.5, n - 0.25, 7.0], [3.0, n, 0.0, 31.5]],
                     dtype=np.float32)
     r = ctx.density(dev(torch, edge), 2.0)

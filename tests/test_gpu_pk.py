@@ -2,7 +2,7 @@
 storage) against the float64 oracle (oracle/torch64.py, the reference algorithm in float64
 on the GPU), started from the same initial conditions.
 
-Gate (the benchmark spec): P(k) within 0.5% for k < k_Nyquist / 2, total mass exact to float32
+Gate: P(k) within 0.5% for k < k_Nyquist / 2, total mass exact to float32
 rounding.  Trajectories themselves are not compared after many steps: N-body dynamics
 amplify rounding differences, the power spectrum is the statistic that must agree."""
 import json
