@@ -451,7 +451,9 @@ def run_reference(args, ws, rank):
             "warmup": min(args.warmup, 1), "ms_per_step": cb["seconds"] * 1e3 / K, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded GRF + Zel'dovich ICs (reference algorithm)",
-            "config": {"workload": WORKLOAD, "n_parts": 256, "n_cells": 512, "box_size": 250.0,
+            "config": {"workload": WORKLOAD if (cfg.n_parts, cfg.n_cells) == (256, 512) else
+                       f"reduced case: {cfg.n_parts}^3 particles, {cfg.n_cells}^3 grid",
+                       "n_parts": cfg.n_parts, "n_cells": cfg.n_cells, "box_size": cfg.box_size,
                        "note": "numba/pyFFTW are not installed: the reference step runs as its CPU port "
                                "(C + OpenMP particle loops, scipy.fft, all host cores); steps bounded to a few "
                                "full-size steps"},

@@ -48,3 +48,25 @@ def test_reference_arm_prints_from_rank_zero_only(capsys):
     args = argparse.Namespace(steps=1, cpu_steps=1, warmup=0, n_parts=8, n_cells=16, box=100.0)
     bench.run_reference(args, 2, 1)
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_contract(capsys):
+    """Rank 0 of the reference arm prints one JSON line carrying the contract keys; its e2e
+    moves no host<->device bytes and its value is the CPU port's."""
+    import argparse
+    import json
+    import bench
+    args = argparse.Namespace(steps=2, cpu_steps=1, warmup=0, n_parts=8, n_cells=16, box=100.0)
+    bench.run_reference(args, 1, 0)
+    lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["steps"] == 1 and d["value"] > 0
+    assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT and d["higher_is_better"] is True
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert (d["config"]["n_parts"], d["config"]["n_cells"], d["config"]["box_size"]) == (8, 16, 100.0)
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1
