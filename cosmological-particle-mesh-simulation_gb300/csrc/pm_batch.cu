@@ -4,13 +4,22 @@
 // structure-of-arrays buffers (double buffered), stored as float32 displacements from
 // their Lagrangian lattice point plus the particle index; every step the kick writes
 // the state back in the order of the step's cell-key sort, so that the next step reads
-// it almost in order.  Simulation s owns the slot range [part_off_s, part_off_s + np_s)
-// and the x-rows [row_base_s, row_base_s + N_s^2) of the common key space, in the same
-// order, so one counting sort over the rows serves the whole batch.  Every phase is one launch
-// over all simulations (the spectral phases: one per distinct grid size).  A step is
-// captured once into a CUDA graph per plan and replayed; the scale factor and the
-// step coefficients advance on the device.
+// it almost in order.  Simulation s owns the x-rows [row_base_s, row_base_s + N_s^2) of the
+// common key space and, in the sorted order (and so in the state a step writes), the range
+// [part_off_s, part_off_s + np_s), in the same order, so one counting sort over the rows
+// serves the whole batch.  Every phase is one launch over all simulations (the spectral
+// phases: one per distinct grid size).  A step is captured once into a CUDA graph per plan
+// and replayed; the scale factor and the step coefficients advance on the device.
+//
+// Admission and retirement do not drain the device.  A new simulation is converted into the
+// free slots after the last one.  A finished one has its final state extracted on the step
+// stream (an event marks its completion) and simply leaves the plan: its slots hold no keys
+// (0xffffffff, skipped by the sort), so the next step's sort and kick write the survivors
+// back compactly -- no copy of the resident state.  Grids of retired simulations are kept
+// for reuse (per grid size) instead of being freed, since cudaFree synchronises the device.
 #include <algorithm>
+#include <chrono>
+#include <cstddef>
 #include <map>
 #include <memory>
 
@@ -30,7 +39,10 @@ struct SimRec {
   bool resident = false;  // particles in the batch arrays
   DBuf grid, spec, rho;   // potential (and density unless keep_density), spectrum, density
   DBuf fin_pos, fin_vel;  // final state once retired (absolute, particle order)
-  long long part_off = 0;
+  cudaEvent_t fin_ev = nullptr;  // recorded after the final state's extraction
+  CUtensorMap maps[2];           // y- and z-pass tensor maps of its spectrum (encoded at admission)
+  long long part_off = 0;  // offset in the sorted order (compact)
+  long long in_off = 0;    // slot offset in the state the next step reads
   unsigned row_base = 0;
 };
 
@@ -48,6 +60,7 @@ struct Plan {
   std::vector<int> fused, fdep_total;    // per distinct size: deposit fused with the x R2C, its tiles
   int max_dep_smem = 0;
   int max_n = 0;
+  long long sort_n = 0;  // slots the next step's sort reads (> ptot right after a retirement)
 };
 
 const int kStateArrays = 11;  // x y z vx vy vz id, cell record: cell fx fy fz
@@ -70,12 +83,29 @@ struct pm_batch {
   DBuf row_start, d_sims, d_prefix, d_err, d_maps;
   DBuf tile_next;   // tile counter of the fused deposit, and 2 words of scratch for the ordering
   DBuf tile_order;  // the fused deposit's tiles, dense first
+  DBuf d_one;       // descriptor + work table of a one-simulation deposit (pm_batch_density)
   DBuf row_count, row_cursor, scan_sums;  // counting sort of the row keys
   Plan plan;
   bool dirty = true, keys_valid = false;
   bool graphs = true;
+  bool sparse = false;      // the state the next step reads has empty slots (after a retirement)
+  long long in_total = 0;   // slots of that state
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-  cudaStream_t own = nullptr;  // used when the caller passes the legacy stream (captures need one)
+  cudaStream_t own = nullptr;     // used when the caller passes the legacy stream (captures need one)
+  cudaStream_t admit = nullptr;   // admission conversions
+  cudaEvent_t last_step = nullptr;  // recorded after the last enqueued step
+  // grids (potential, spectrum) of retired simulations by grid size, and final-state
+  // buffers by particle count, kept for reuse
+  std::map<int, std::vector<std::pair<DBuf, DBuf>>> grid_pool;
+  std::map<long long, std::vector<std::pair<DBuf, DBuf>>> fin_pool;
+  DBuf stage_pos, stage_vel;  // admission staging of host initial conditions
+  // pinned host staging of the plan's uploads (two, used in turn; an event marks when the
+  // device has read one), so that re-planning never waits for enqueued work
+  void* plan_host[2] = {nullptr, nullptr};
+  size_t plan_host_bytes[2] = {0, 0};
+  cudaEvent_t plan_ev[2] = {nullptr, nullptr};
+  int plan_turn = 0;
+  double host_s[4] = {0, 0, 0, 0};  // host seconds: admission, planning, graph capture, retirement
   std::string err;
 };
 
@@ -138,19 +168,58 @@ size_t used_bytes(pm_batch* b) {
   return u;
 }
 
-cudaError_t grow_state(pm_batch* b, long long need, cudaStream_t st) {
+// Device bytes held for reuse (grids and final-state buffers of simulations that left).
+size_t pooled_bytes(pm_batch* b) {
+  size_t u = 0;
+  for (auto& e : b->grid_pool)
+    for (auto& g : e.second) u += g.first.bytes + g.second.bytes;
+  for (auto& e : b->fin_pool)
+    for (auto& g : e.second) u += g.first.bytes + g.second.bytes;
+  return u;
+}
+
+// Frees pooled buffers until `need` more bytes fit under the cap next to what is in use
+// (cudaFree synchronises the device: only when memory is short).
+void trim_pools(pm_batch* b, size_t need) {
+  if (!b->cap) return;
+  auto over = [&]() { return used_bytes(b) + pooled_bytes(b) + need > b->cap; };
+  for (auto& e : b->grid_pool)
+    while (over() && !e.second.empty()) {
+      e.second.back().first.release();
+      e.second.back().second.release();
+      e.second.pop_back();
+    }
+  for (auto& e : b->fin_pool)
+    while (over() && !e.second.empty()) {
+      e.second.back().first.release();
+      e.second.back().second.release();
+      e.second.pop_back();
+    }
+}
+
+// Accumulates the host time of a scope into one of pm_batch::host_s.
+struct HostTimer {
+  double& acc;
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  explicit HostTimer(double& a) : acc(a) {}
+  ~HostTimer() { acc += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+// Room for `need` slots; the current state's first in_total slots are kept (rare: capacity
+// grows by half each time, after the device has finished all enqueued work).
+cudaError_t grow_state(pm_batch* b, long long need) {
   if (need <= b->pcap) return cudaSuccess;
   long long cap = std::max(need, b->pcap + b->pcap / 2);
-  const long long keep = resident_particles(b);
+  const long long keep = b->in_total;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e) return e;
   for (int w = 0; w < 2; ++w) {
     for (int k = 0; k < kStateArrays; ++k) {
       DBuf nb;
-      cudaError_t e = nb.ensure((size_t)cap * 4);
+      e = nb.ensure((size_t)cap * 4);
       if (e) return e;
       if (w == b->cur && keep > 0 && b->st[w][k].p) {
-        e = cudaMemcpyAsync(nb.p, b->st[w][k].p, (size_t)keep * 4, cudaMemcpyDeviceToDevice, st);
-        if (e) return e;
-        e = cudaStreamSynchronize(st);
+        e = cudaMemcpy(nb.p, b->st[w][k].p, (size_t)keep * 4, cudaMemcpyDeviceToDevice);
         if (e) return e;
       }
       b->st[w][k].release();
@@ -158,6 +227,7 @@ cudaError_t grow_state(pm_batch* b, long long need, cudaStream_t st) {
     }
   }
   b->pcap = cap;
+  b->keys_valid = false;  // the sort buffers are reallocated
   return b->sort.ensure(cap);
 }
 
@@ -182,6 +252,7 @@ Lattice* lattice_for(pm_batch* b, int np1, int n) {
 
 // Build the plan (Sim descriptors, work prefixes) for the resident simulations.
 int build_plan(pm_batch* b, cudaStream_t st) {
+  HostTimer timer(b->host_s[1]);
   Plan& P = b->plan;
   P = Plan();
   P.nsims = (int)b->sims.size();
@@ -206,6 +277,7 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   }
   P.ptot = off;
   P.rows = rows;
+  P.sort_n = b->sparse ? b->in_total : P.ptot;
   P.bits = ceil_log2((long long)rows) + P.xbits;  // keys are < rows
   if (P.bits > 32) return bfail(b, PM_ERR_ADMIT, "batch key space exceeds 32 bits");
   std::sort(P.sizes.begin(), P.sizes.end());
@@ -230,6 +302,7 @@ int build_plan(pm_batch* b, cudaStream_t st) {
     d.tz = TILE_Z;
     d.np = r.np;
     d.part_off = r.part_off;
+    d.slot_off = r.in_off;
     d.row_base = r.row_base;
     d.phi = r.grid.as<float>();
     d.rho = (r.cfg.flags & PM_FLAG_KEEP_DENSITY) ? r.rho.as<float>() : r.grid.as<float>();
@@ -279,30 +352,45 @@ int build_plan(pm_batch* b, cudaStream_t st) {
       if (b->sims[i]->n == P.sizes[g]) { only = i; ++count; }
     P.single.push_back(count == 1 ? only : -1);
   }
-  {  // tensor maps of every spectrum (y pass, z pass) for the TMA line passes
-    std::vector<CUtensorMap> maps(2 * (size_t)S);
-    std::memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
-    for (int i = 0; i < S; ++i) spectral_encode_maps(b->sims[i]->n, b->sims[i]->spec.p, &maps[2 * i]);
-    PB_CK(b->d_maps.ensure(sizeof(CUtensorMap) * maps.size()), "alloc maps");
-    PB_CK(cudaMemcpyAsync(b->d_maps.p, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice, st),
-          "upload maps");
-  }
-  PB_CK(b->d_sims.ensure(sizeof(Sim) * S), "alloc sims");
-  PB_CK(b->d_prefix.ensure(sizeof(int) * pre.size()), "alloc prefix");
-  PB_CK(b->row_start.ensure(sizeof(unsigned) * ((size_t)rows + 1)), "alloc rows");
-  PB_CK(b->row_count.ensure(sizeof(unsigned) * (size_t)rows), "alloc rows");
+  PB_CK(b->d_maps.ensure_geo(sizeof(CUtensorMap) * 2 * (size_t)S), "alloc maps");
+  PB_CK(b->d_sims.ensure_geo(sizeof(Sim) * S), "alloc sims");
+  PB_CK(b->d_prefix.ensure_geo(sizeof(int) * pre.size()), "alloc prefix");
+  PB_CK(b->row_start.ensure_geo(sizeof(unsigned) * ((size_t)rows + 1)), "alloc rows");
+  PB_CK(b->row_count.ensure_geo(sizeof(unsigned) * (size_t)rows), "alloc rows");
   {
     size_t tiles = 1;
     for (int t : P.fdep_total) tiles = std::max(tiles, (size_t)t);
-    PB_CK(b->tile_order.ensure(sizeof(unsigned) * tiles), "alloc tile order");
+    PB_CK(b->tile_order.ensure_geo(sizeof(unsigned) * tiles), "alloc tile order");
   }
-  PB_CK(b->row_cursor.ensure(sizeof(unsigned) * (size_t)rows), "alloc rows");
-  PB_CK(b->scan_sums.ensure(sizeof(unsigned) * row_sort_block_sums(rows)), "alloc rows");
-  PB_CK(cudaMemcpyAsync(b->d_sims.p, hs.data(), sizeof(Sim) * S, cudaMemcpyHostToDevice, st), "upload sims");
-  PB_CK(cudaMemcpyAsync(b->d_prefix.p, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice, st),
-        "upload prefix");
+  PB_CK(b->row_cursor.ensure_geo(sizeof(unsigned) * (size_t)rows), "alloc rows");
+  PB_CK(b->scan_sums.ensure_geo(sizeof(unsigned) * row_sort_block_sums(rows)), "alloc rows");
+  {  // tensor maps (for the TMA line passes), descriptors and work prefixes, through pinned staging
+    const size_t mb = sizeof(CUtensorMap) * 2 * (size_t)S, sbytes = sizeof(Sim) * S, pbytes = sizeof(int) * pre.size();
+    const size_t o_sims = (mb + 255) / 256 * 256, o_pre = o_sims + (sbytes + 255) / 256 * 256, total = o_pre + pbytes;
+    const int t = b->plan_turn;
+    if (!b->plan_ev[t]) PB_CK(cudaEventCreateWithFlags(&b->plan_ev[t], cudaEventDisableTiming), "event");
+    else PB_CK(cudaEventSynchronize(b->plan_ev[t]), "staging");  // its last uploads have been read
+    if (b->plan_host_bytes[t] < total) {
+      if (b->plan_host[t]) cudaFreeHost(b->plan_host[t]);
+      b->plan_host[t] = nullptr;
+      b->plan_host_bytes[t] = 0;
+      const size_t want = std::max(total, (size_t)64 << 10);
+      PB_CK(cudaMallocHost(&b->plan_host[t], want), "alloc staging");
+      b->plan_host_bytes[t] = want;
+    }
+    char* h = static_cast<char*>(b->plan_host[t]);
+    for (int i = 0; i < S; ++i) std::memcpy(h + sizeof(CUtensorMap) * 2 * i, b->sims[i]->maps, sizeof(CUtensorMap) * 2);
+    std::memcpy(h + o_sims, hs.data(), sbytes);
+    std::memcpy(h + o_pre, pre.data(), pbytes);
+    PB_CK(cudaMemcpyAsync(b->d_maps.p, h, mb, cudaMemcpyHostToDevice, st), "upload maps");
+    PB_CK(cudaMemcpyAsync(b->d_sims.p, h + o_sims, sbytes, cudaMemcpyHostToDevice, st), "upload sims");
+    PB_CK(cudaMemcpyAsync(b->d_prefix.p, h + o_pre, pbytes, cudaMemcpyHostToDevice, st), "upload prefix");
+    PB_CK(cudaEventRecord(b->plan_ev[t], st), "event");
+    b->plan_turn = 1 - t;
+  }
   PB_CK(launch_coef(b->d_sims.as<Sim>(), S, 0, st), "coef");
-  PB_CK(cudaStreamSynchronize(st), "plan sync");
+  // (the uploads are ordered on `st` after the steps already enqueued: pageable host memory is
+  // staged before cudaMemcpyAsync returns, so no synchronisation is needed here)
   for (size_t g = 0; g < P.sizes.size(); ++g) {
     PB_CK(spectral_dispatch(SPEC_PREPARE, P.sizes[g], nullptr, Work(), 0, st), "prepare");
     if (P.fused[g])
@@ -340,7 +428,7 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
   // group the particles by x-row: row starts and the permutation to row order
   unsigned* perm = b->sort.vals.as<unsigned>();
   // (the row histogram of the keys was made by the previous kick, or by ensure_keys)
-  PB_CK(row_counting_sort(b->sort.keys.as<unsigned>(), P.ptot, P.rows, b->row_count.as<unsigned>(),
+  PB_CK(row_counting_sort(b->sort.keys.as<unsigned>(), P.sort_n, P.rows, b->row_count.as<unsigned>(),
                           b->row_start.as<unsigned>(), b->row_cursor.as<unsigned>(), b->scan_sums.as<unsigned>(),
                           perm, err, b->sms, st, nullptr, true),
         "sort");
@@ -402,22 +490,34 @@ int launches_per_step(pm_batch* b) {
 int ensure_keys(pm_batch* b, cudaStream_t st) {
   if (b->keys_valid) return PM_OK;
   Plan& P = b->plan;
+  // slots without a resident particle (left by retired simulations) hold no key
+  PB_CK(cudaMemsetAsync(b->sort.keys.p, 0xff, sizeof(unsigned) * (size_t)P.sort_n, st), "clear keys");
   PB_CK(launch_keys_disp(b->d_sims.as<Sim>(), work_of(b, PH_KEYS, P.fixed_total[PH_KEYS]), state(b, b->cur),
                          b->sort.keys.as<unsigned>(), nullptr, b->d_err.as<int>(),
                          grid_for(P.fixed_total[PH_KEYS], b->sms, 16), st),
         "keys");
-  PB_CK(row_histogram(b->sort.keys.as<unsigned>(), P.ptot, P.rows, b->row_count.as<unsigned>(), b->d_err.as<int>(),
+  PB_CK(row_histogram(b->sort.keys.as<unsigned>(), P.sort_n, P.rows, b->row_count.as<unsigned>(), b->d_err.as<int>(),
                       b->sms, st),
         "row histogram");
   b->keys_valid = true;
   return PM_OK;
 }
 
+// After a step the state is compact: every simulation's slots are its sorted range.
+void compacted(pm_batch* b) {
+  if (!b->sparse) return;
+  b->sparse = false;
+  for (auto& s : b->sims) s->in_off = s->part_off;
+  b->in_total = b->plan.ptot;
+  b->plan.sort_n = b->plan.ptot;
+}
+
 int run_steps(pm_batch* b, int k, cudaStream_t st) {
   for (int i = 0; i < k; ++i) {
     const int cur = b->cur;
-    if (b->graphs) {
+    if (b->graphs && !b->sparse) {
       if (!b->gexec[cur]) {
+        HostTimer timer(b->host_s[2]);
         cudaGraph_t g = nullptr;
         PB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
         const int r = enqueue_step(b, cur, st);
@@ -433,50 +533,61 @@ int run_steps(pm_batch* b, int k, cudaStream_t st) {
       }
       PB_CK(cudaGraphLaunch(b->gexec[cur], st), "graph launch");
     } else {
+      // (the first step after a retirement reads a state with empty slots: launched directly,
+      // the graphs are captured for the compact state that follows)
       if (int r = enqueue_step(b, cur, st)) return r;
     }
     b->cur = 1 - cur;
+    compacted(b);
   }
   return PM_OK;
 }
 
-// Copy the final state of finished simulations out and compact the others.
+// Finished simulations leave the batch: their final state is extracted on `st` (fin_ev marks
+// its completion) and their grids go to the pool.  The others stay where they are; the next
+// step's sort skips the empty slots and its kick writes the survivors back compactly.
 int retire_finished(pm_batch* b, cudaStream_t st) {
   bool any = false;
   for (auto& s : b->sims) any |= s->done >= s->nsteps;
   if (!any) return PM_OK;
+  HostTimer timer(b->host_s[3]);
   Parts curp = state(b, b->cur);
   std::vector<std::unique_ptr<SimRec>> keep;
-  long long off = 0;
-  const int dst = 1 - b->cur;
   for (auto& s : b->sims) {
     if (s->done >= s->nsteps) {
       const size_t pb = (size_t)3 * s->np * sizeof(float);
+      auto& fp = b->fin_pool[s->np];
+      if (!fp.empty()) {
+        s->fin_pos = fp.back().first;
+        s->fin_vel = fp.back().second;
+        fp.pop_back();
+      }
       PB_CK(s->fin_pos.ensure(pb), "alloc final");
       PB_CK(s->fin_vel.ensure(pb), "alloc final");
       Lattice* l = lattice_for(b, s->np1, s->n);
-      PB_CK(launch_disp_to_abs(curp, s->part_off, s->np, s->np1, s->n, l->qi.as<int>(), l->qf.as<float>(),
+      PB_CK(launch_disp_to_abs(curp, s->in_off, s->np, s->np1, s->n, l->qi.as<int>(), l->qf.as<float>(),
                                s->fin_pos.as<float>(), s->fin_vel.as<float>(), st),
             "extract");
+      if (!s->fin_ev) PB_CK(cudaEventCreateWithFlags(&s->fin_ev, cudaEventDisableTiming), "event");
+      PB_CK(cudaEventRecord(s->fin_ev, st), "event");
       s->resident = false;
-      s->grid.release();
-      s->spec.release();
+      b->grid_pool[s->n].emplace_back(s->grid, s->spec);  // reused in stream order on `st`
+      s->grid = DBuf();
+      s->spec = DBuf();
       s->rho.release();
       b->retired.push_back(std::move(s));
+      b->sparse = true;
     } else {
-      for (int k = 0; k < kStateArrays; ++k)
-        PB_CK(cudaMemcpyAsync(b->st[dst][k].as<char>() + off * 4, b->st[b->cur][k].as<char>() + s->part_off * 4,
-                              (size_t)s->np * 4, cudaMemcpyDeviceToDevice, st),
-              "compact");
-      off += s->np;
       keep.push_back(std::move(s));
     }
   }
-  PB_CK(cudaStreamSynchronize(st), "retire sync");
   b->sims = std::move(keep);
-  b->cur = dst;
   b->dirty = true;
   b->keys_valid = false;
+  if (b->sims.empty()) {  // nothing left to read: the next admission starts a fresh state
+    b->sparse = false;
+    b->in_total = 0;
+  }
   return PM_OK;
 }
 
@@ -513,6 +624,8 @@ int pm_batch_create(int device, size_t mem_cap_bytes, pm_batch** out) {
   if (!e) e = b->tile_next.ensure(4 * sizeof(unsigned));
   if (!e) e = cudaMemset(b->d_err.p, 0, sizeof(int));
   if (!e) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
+  if (!e) e = cudaStreamCreateWithFlags(&b->admit, cudaStreamNonBlocking);
+  if (!e) e = cudaEventCreateWithFlags(&b->last_step, cudaEventDisableTiming);
   if (!e) e = cudaDeviceSynchronize();
   if (e) {
     pm_batch_destroy(b);
@@ -532,7 +645,14 @@ void pm_batch_destroy(pm_batch* b) {
   }
   for (auto& s : b->retired) {
     s->fin_pos.release(); s->fin_vel.release();
+    if (s->fin_ev) cudaEventDestroy(s->fin_ev);
   }
+  for (auto& e : b->grid_pool)
+    for (auto& g : e.second) { g.first.release(); g.second.release(); }
+  for (auto& e : b->fin_pool)
+    for (auto& g : e.second) { g.first.release(); g.second.release(); }
+  b->stage_pos.release();
+  b->stage_vel.release();
   for (auto& t : b->tables) t.second->release();
   for (auto& l : b->lattices) l.second->release();
   b->sort.release();
@@ -546,7 +666,14 @@ void pm_batch_destroy(pm_batch* b) {
   b->tile_next.release();
   b->tile_order.release();
   b->d_maps.release();
+  b->d_one.release();
   if (b->own) cudaStreamDestroy(b->own);
+  if (b->admit) cudaStreamDestroy(b->admit);
+  for (int t = 0; t < 2; ++t) {
+    if (b->plan_ev[t]) cudaEventDestroy(b->plan_ev[t]);
+    if (b->plan_host[t]) cudaFreeHost(b->plan_host[t]);
+  }
+  if (b->last_step) cudaEventDestroy(b->last_step);
   delete b;
 }
 
@@ -574,7 +701,6 @@ int pm_batch_add(pm_batch* b, const pm_config* cfg, const float* positions, cons
     return bfail(b, PM_ERR_ARG, "bad time range");
   const size_t need = footprint(*cfg);
   if (b->cap && used_bytes(b) + need > b->cap) return bfail(b, PM_ERR_ADMIT, "memory cap reached");
-  cudaStream_t st = nullptr;
   std::unique_ptr<SimRec> r(new SimRec());
   r->id = b->next_id++;
   r->cfg = *cfg;
@@ -589,34 +715,50 @@ int pm_batch_add(pm_batch* b, const pm_config* cfg, const float* positions, cons
     while (a < cfg->a_end - r->da) { a += r->da; ++k; }
     r->nsteps = k;
   }
+  HostTimer timer(b->host_s[0]);
   const size_t gb = (size_t)r->n * r->n * r->n * sizeof(float);
-  PB_CK(r->grid.ensure(gb), "alloc grid");
+  const size_t sb = (size_t)r->n * r->n * spec_pitch(r->n) * sizeof(float2);
+  auto& gp = b->grid_pool[r->n];
+  if (!gp.empty()) {  // a retired simulation's grids (stream-ordered reuse by the next step)
+    r->grid = gp.back().first;
+    r->spec = gp.back().second;
+    gp.pop_back();
+  } else {
+    trim_pools(b, gb + sb);
+    PB_CK(r->grid.ensure(gb), "alloc grid");
+    PB_CK(r->spec.ensure(sb), "alloc spectrum");
+  }
   if (cfg->flags & PM_FLAG_KEEP_DENSITY) PB_CK(r->rho.ensure(gb), "alloc density");
-  PB_CK(r->spec.ensure((size_t)r->n * r->n * spec_pitch(r->n) * sizeof(float2)), "alloc spectrum");
+  std::memset(r->maps, 0, sizeof(r->maps));
+  spectral_encode_maps(r->n, r->spec.p, r->maps);
   PB_CK(tables_for(b, r->n)->build(r->n), "tables");
   Lattice* l = lattice_for(b, r->np1, r->n);
   PB_CK(l->build(r->np1, r->n), "lattice");
-  const long long off = resident_particles(b);
-  PB_CK(grow_state(b, off + r->np, st), "alloc state");
+  // the new simulation takes the slots after the last ones of the state the next step reads
+  const long long off = b->in_total;
+  PB_CK(grow_state(b, off + r->np), "alloc state");
+  // Convert on the admission stream once the steps already enqueued are done (an earlier
+  // step may still write these slots), and wait for it here: the caller's arrays are free
+  // when this returns.
+  cudaStream_t st = b->admit;
+  PB_CK(cudaStreamWaitEvent(st, b->last_step, 0), "wait steps");
   const float* dp = positions;
   const float* dv = velocities;
-  DBuf tp, tv;
   const size_t pb = (size_t)3 * r->np * sizeof(float);
   if (!on_device) {
-    PB_CK(tp.ensure(pb), "alloc staging");
-    PB_CK(tv.ensure(pb), "alloc staging");
-    PB_CK(cudaMemcpy(tp.p, positions, pb, cudaMemcpyHostToDevice), "h2d");
-    PB_CK(cudaMemcpy(tv.p, velocities, pb, cudaMemcpyHostToDevice), "h2d");
-    dp = tp.as<float>();
-    dv = tv.as<float>();
+    PB_CK(b->stage_pos.ensure_geo(pb), "alloc staging");
+    PB_CK(b->stage_vel.ensure_geo(pb), "alloc staging");
+    PB_CK(cudaMemcpyAsync(b->stage_pos.p, positions, pb, cudaMemcpyHostToDevice, st), "h2d");
+    PB_CK(cudaMemcpyAsync(b->stage_vel.p, velocities, pb, cudaMemcpyHostToDevice, st), "h2d");
+    dp = b->stage_pos.as<float>();
+    dv = b->stage_vel.as<float>();
   }
   PB_CK(launch_abs_to_disp(dp, dv, r->np, r->np1, r->n, l->qi.as<int>(), l->qf.as<float>(), state(b, b->cur), off,
                            st),
         "convert");
   PB_CK(cudaStreamSynchronize(st), "sync");
-  tp.release();
-  tv.release();
-  r->part_off = off;
+  r->in_off = off;
+  b->in_total = off + r->np;
   r->resident = true;
   *sim_id = r->id;
   b->sims.push_back(std::move(r));
@@ -649,6 +791,7 @@ int pm_batch_step(pm_batch* b, int nsteps, void* stream) {
     left -= k;
   }
   const int r = retire_finished(b, st);
+  if (r == PM_OK) PB_CK(cudaEventRecord(b->last_step, st), "event");
   if (!stream && r == PM_OK) PB_CK(cudaStreamSynchronize(st), "sync");
   return r;
 }
@@ -656,9 +799,15 @@ int pm_batch_step(pm_batch* b, int nsteps, void* stream) {
 int pm_batch_active(pm_batch* b, int sim_id) {
   if (!b) return -1;
   for (auto& s : b->sims)
-    if (s->id == sim_id) return s->done < s->nsteps ? 1 : 0;
+    if (s->id == sim_id) return 1;
   for (auto& s : b->retired)
-    if (s->id == sim_id) return 0;
+    if (s->id == sim_id) {
+      if (!s->fin_ev) return 0;
+      const cudaError_t q = cudaEventQuery(s->fin_ev);
+      if (q == cudaErrorNotReady) return 1;  // its last steps are still running on the device
+      if (q != cudaSuccess) cudaGetLastError();  // reported by the next call that synchronises
+      return 0;
+    }
   return -1;
 }
 
@@ -675,11 +824,13 @@ int pm_batch_get(pm_batch* b, int sim_id, float* positions, float* velocities, i
   const float* sp;
   const float* sv;
   DBuf tp, tv;
+  // after the steps enqueued on the batch's stream (and the final-state extraction)
+  PB_CK(cudaStreamWaitEvent(st, s->resident || !s->fin_ev ? b->last_step : s->fin_ev, 0), "wait");
   if (s->resident) {
     PB_CK(tp.ensure(pb), "alloc staging");
     PB_CK(tv.ensure(pb), "alloc staging");
     Lattice* l = lattice_for(b, s->np1, s->n);
-    PB_CK(launch_disp_to_abs(state(b, b->cur), s->part_off, s->np, s->np1, s->n, l->qi.as<int>(),
+    PB_CK(launch_disp_to_abs(state(b, b->cur), s->in_off, s->np, s->np1, s->n, l->qi.as<int>(),
                              l->qf.as<float>(), tp.as<float>(), tv.as<float>(), st),
           "extract");
     sp = tp.as<float>();
@@ -697,12 +848,65 @@ int pm_batch_get(pm_batch* b, int sim_id, float* positions, float* velocities, i
   return read_back_a(b, st);
 }
 
+int pm_batch_density(pm_batch* b, int sim_id, float* rho, void* stream) {
+  if (!b) return PM_ERR_ARG;
+  if (!rho) return bfail(b, PM_ERR_ARG, "null array");
+  cudaStream_t st = stream ? (cudaStream_t)stream : b->own;
+  if (!stream) PB_CK(cudaDeviceSynchronize(), "sync");
+  int idx = -1;
+  for (size_t i = 0; i < b->sims.size(); ++i)
+    if (b->sims[i]->id == sim_id) idx = (int)i;
+  if (idx < 0) return bfail(b, PM_ERR_ARG, find_sim(b, sim_id) ? "simulation is no longer resident" : "unknown simulation id");
+  if (b->dirty) {
+    if (int r = build_plan(b, st)) return r;
+  }
+  if (int r = ensure_keys(b, st)) return r;
+  const Plan& P = b->plan;
+  // group the batch's particles by row from the current keys (the row histogram the last kick
+  // or ensure_keys made is only read: the next step's sort finds it unchanged)
+  unsigned* perm = b->sort.vals.as<unsigned>();
+  int* err = b->d_err.as<int>();
+  PB_CK(cudaStreamWaitEvent(st, b->last_step, 0), "wait");
+  PB_CK(row_counting_sort(b->sort.keys.as<unsigned>(), P.sort_n, P.rows, b->row_count.as<unsigned>(),
+                          b->row_start.as<unsigned>(), b->row_cursor.as<unsigned>(), b->scan_sums.as<unsigned>(),
+                          perm, err, b->sms, st, nullptr, true),
+        "sort");
+  // this simulation's descriptor with the caller's grid as the deposit's output
+  Sim s{};
+  PB_CK(cudaMemcpyAsync(&s, b->d_sims.as<Sim>() + idx, sizeof(Sim), cudaMemcpyDeviceToHost, st), "read sim");
+  PB_CK(cudaStreamSynchronize(st), "sync");
+  s.rho = rho;
+  struct {
+    Sim sim;
+    int prefix[2];
+  } one{s, {0, (s.n / TILE_Y) * (s.n / TILE_Z)}};
+  PB_CK(b->d_one.ensure(sizeof(one)), "alloc descriptor");
+  PB_CK(cudaMemcpy(b->d_one.p, &one, sizeof(one), cudaMemcpyHostToDevice), "upload descriptor");
+  auto* d = b->d_one.as<char>();
+  const Work w{reinterpret_cast<const int*>(d + offsetof(decltype(one), prefix)), 1, one.prefix[1]};
+  PB_CK(launch_deposit(reinterpret_cast<const Sim*>(d), w, state(b, b->cur), perm, b->row_start.as<unsigned>(),
+                       POS_DISP, err, grid_for(one.prefix[1], b->sms, 3), deposit_smem_bytes(s.n, TILE_Y, TILE_Z),
+                       st),
+        "deposit");
+  PB_CK(cudaEventRecord(b->last_step, st), "event");
+  if (!stream) PB_CK(cudaStreamSynchronize(st), "sync");
+  return PM_OK;
+}
+
 int pm_batch_remove(pm_batch* b, int sim_id) {
   if (!b) return PM_ERR_ARG;
   for (size_t i = 0; i < b->retired.size(); ++i) {
-    if (b->retired[i]->id == sim_id) {
-      b->retired[i]->fin_pos.release();
-      b->retired[i]->fin_vel.release();
+    SimRec& r = *b->retired[i];
+    if (r.id == sim_id) {
+      // its buffers are reused in the order of the batch's stream, after the extraction
+      if (r.fin_ev) {
+        PB_CK(cudaEventSynchronize(r.fin_ev), "sync");
+        cudaEventDestroy(r.fin_ev);
+        r.fin_ev = nullptr;
+      }
+      if (r.fin_pos.p) b->fin_pool[r.np].emplace_back(r.fin_pos, r.fin_vel);
+      r.fin_pos = DBuf();
+      r.fin_vel = DBuf();
       b->retired.erase(b->retired.begin() + i);
       return PM_OK;
     }
@@ -710,12 +914,18 @@ int pm_batch_remove(pm_batch* b, int sim_id) {
   for (auto& s : b->sims) {
     if (s->id == sim_id) {
       s->done = s->nsteps;  // retire now, then drop
-      cudaStream_t st = nullptr;
-      if (int r = retire_finished(b, st)) return r;
+      if (int r = retire_finished(b, b->own)) return r;
+      PB_CK(cudaEventRecord(b->last_step, b->own), "event");
       return pm_batch_remove(b, sim_id);
     }
   }
   return bfail(b, PM_ERR_ARG, "unknown simulation id");
+}
+
+int pm_batch_host_seconds(pm_batch* b, double* out, int n) {
+  if (!b || !out || n < 0) return PM_ERR_ARG;
+  for (int i = 0; i < n && i < 4; ++i) out[i] = b->host_s[i];
+  return PM_OK;
 }
 
 int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void* stream) {
@@ -738,6 +948,7 @@ int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void*
     rc = enqueue_step(b, b->cur, st, ev);
     if (rc) break;
     b->cur = 1 - b->cur;
+    compacted(b);
     for (auto& s : b->sims) { s->a += s->da; s->done += 1; }
     cudaError_t e = cudaEventSynchronize(ev[PP_COUNT]);
     if (e) { rc = bcuda(b, e, "profile sync"); break; }
@@ -749,7 +960,9 @@ int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void*
   }
   for (auto& e : ev) cudaEventDestroy(e);
   if (rc) return rc;
-  return retire_finished(b, st);
+  const int r = retire_finished(b, st);
+  if (r == PM_OK) PB_CK(cudaEventRecord(b->last_step, st), "event");
+  return r;
 }
 
 int pm_batch_launches_per_step(pm_batch* b) {

@@ -13,10 +13,50 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+#include <mutex>
+
 #define PM_FIX_BITS 26          // CIC weights are accumulated as integers w * 2^26
 #define PM_MAX_N 1024
 
 namespace pm {
+
+constexpr int PM_MAX_DEVICES = 64;
+
+// Kernel attributes (dynamic shared-memory limits, carve-outs) are state of each device,
+// not of the process: DeviceOnce runs a set-up function once for every device it is called
+// on (the current device), under a lock, and remembers the devices whose set-up succeeded.
+struct DeviceOnce {
+  std::atomic<unsigned long long> done{0};
+  std::mutex m;
+  template <class F>
+  cudaError_t run(F fn) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if (dev < 0 || dev >= PM_MAX_DEVICES) return cudaErrorInvalidDevice;
+    const unsigned long long bit = 1ull << dev;
+    if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+    std::lock_guard<std::mutex> g(m);
+    if (done.load(std::memory_order_relaxed) & bit) return cudaSuccess;
+    e = fn();
+    if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+    return e;
+  }
+};
+
+// Streaming multiprocessors of the current device (cached per device).
+inline int device_sms() {
+  static std::atomic<int> cache[PM_MAX_DEVICES];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= PM_MAX_DEVICES) return 1;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
 
 enum : int {
   ERR_OK = 0,
@@ -38,7 +78,10 @@ struct Sim {
   int flags;
   int q_step;       // n / np1 when np1 divides n (lattice q = q_step i + 1/2); 0: use the tables
   long long np;        // particle count
-  long long part_off;  // first particle slot in the batch particle arrays
+  long long part_off;  // first position of this simulation in the sorted order (and in the
+                       // state the kick writes: the batch particle arrays after a step)
+  long long slot_off;  // first particle slot of this simulation in the state being read by the
+                       // keys kernel (differs from part_off right after a retirement)
   unsigned row_base;   // first global row number of this simulation
   unsigned pad1;
   float* rho;          // density n^3 (output of the deposit)
@@ -158,7 +201,7 @@ cudaError_t launch_coef(Sim* sims, int nsims, int advance, cudaStream_t st);
 // vel is null)
 cudaError_t launch_gather_state(const float* pos, const float* vel, long long np, const unsigned* idx, float* spos,
                                 float* svel, int sms, cudaStream_t st);
-cudaError_t deposit_prepare();  // sets kernel attributes (call before graph capture)
+cudaError_t deposit_prepare();  // sets kernel attributes of the current device (call before graph capture)
 // order of the fused deposit's tiles (dense tiles first); counts: 2 device words of scratch
 cudaError_t launch_tile_order(const Sim* sims, const Work& w, const unsigned* row_start, unsigned* order,
                               unsigned* counts, int sms, cudaStream_t st);
@@ -180,6 +223,8 @@ constexpr int SORT_TILE = 4096;
 size_t sort_scratch_hist_entries(long long n);
 constexpr int SORT_DIGIT_TOTALS = 512;  // entries of SortScratch::digit_tot
 int radix_sort_passes(int bits);
+// sets the sort's kernel attributes on the current device (once per device; radix_sort calls it)
+cudaError_t sort_prepare();
 // Sorts keys[0,n) / vals[0,n) on key bits [begin_bit, begin_bit + bits).  Returns via
 // *in_alt whether the result sits in the scratch (alt) buffers.  When gen_vals is set,
 // vals are not read on the first pass and the identity 0..n-1 is used instead.

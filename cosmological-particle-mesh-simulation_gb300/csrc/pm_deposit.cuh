@@ -3,10 +3,9 @@
 // A tile is TZ x TY full x-rows.  The particles whose base cell lies in the tile's source
 // rows (the tile plus one row and one plane below, periodic: 7 runs of the row-sorted
 // order) are found through the row starts; their CIC weights that land inside the tile are
-// added to
-// integer accumulators in shared memory: weights quantised to 2^-26, a 32-bit low word
-// with carry into a 32-bit high word.  Integer sums do not depend on the order of the
-// atomics, so the deposit is bit-identical run to run.
+// added to integer accumulators in shared memory (TileSum: one 32-bit word per cell where the
+// tile's particle count allows, else a low word and a coarse word).  Integer sums do not
+// depend on the order of the atomics, so the deposit is bit-identical run to run.
 #pragma once
 #include "pm_cells.cuh"
 
@@ -22,16 +21,63 @@ __device__ __forceinline__ void acc_add(unsigned* lo, unsigned* co, int i, unsig
   atomicAdd(&co[i], q >> COARSE_SHIFT);
 }
 
-// The exact sum from its low word and its coarse sum, times scale.
+// The exact sum V from its low word l and its coarse sum c, rounded to float32, times scale.
+// V - (c << 12) lies in [0, 2^32), so V = (c << 12) + (l - (c << 12) mod 2^32): its low word
+// is l and its high word is c >> 20 plus the carry of that addition.  V < 2^44, so
+// V = a 2^23 + b with a, b < 2^23; each is exact as a float (2^23 + a has a as its
+// mantissa), and fmaf(a, 2^23, b) rounds once: the value of a round-to-nearest 64-bit
+// conversion, computed on the FP32 pipe (GB300 issues 64-bit integer conversions to its
+// narrow FP64 pipe).
 __device__ __forceinline__ float fixed_to_float(unsigned l, unsigned c, float scale) {
-  const unsigned long long est = (unsigned long long)c << COARSE_SHIFT;
-  return __ull2float_rn(est + (unsigned)(l - (unsigned)est)) * scale;
+  const unsigned est_lo = c << COARSE_SHIFT;
+  const unsigned hi = (c >> (32 - COARSE_SHIFT)) + (l < est_lo ? 1u : 0u);
+  const unsigned a = (hi << 9) | (l >> 23), b = l & 0x7fffffu;
+  const float fa = __uint_as_float(0x4B000000u | a) - 8388608.f;
+  const float fb = __uint_as_float(0x4B000000u | b) - 8388608.f;
+  return fmaf(fa, 8388608.f, fb) * scale;
+}
+
+// How a tile's sums are held.  Every corner weight is quantised to an integer q <= 2^s and
+// added with integer atomics, so a cell's sum -- and the float made from it -- does not depend
+// on the order of the additions.  A cell receives at most one corner from each source entry
+// of its tile, so its sum is at most total * 2^s: a tile with total < 2^(32 - s) sums in one
+// 32-bit word per cell (one atomic per corner).  Tiles whose count allows s >= ONE_WORD_MIN
+// use one word at the largest such s (at most 26); denser tiles sum at 2^-26 in a low word
+// plus a coarse word (two atomics per corner).
+constexpr int ONE_WORD_MIN = 20;
+
+struct TileSum {
+  int s;     // one-word quantisation 2^s; 0: two-word sums at 2^-26
+  float ms;  // particle mass * 2^-(quantisation bits): the float of a sum times ms is its mass
+};
+
+__device__ __forceinline__ TileSum tile_sum(unsigned total, float mass_scale) {
+  const int bits = 32 - __clz(total);  // total < 2^bits
+  const int s = min(PM_FIX_BITS, 32 - bits);
+  TileSum t;
+  t.s = s >= ONE_WORD_MIN ? s : 0;
+  // mass_scale = mass * 2^-26; one-word sums at 2^-s: times 2^(26 - s), exactly
+  t.ms = t.s ? mass_scale * __uint_as_float((unsigned)(127 + PM_FIX_BITS - t.s) << 23) : mass_scale;
+  return t;
+}
+
+// A one-word sum as a float, times scale (exact split l = a 2^23 + b, one rounding).
+__device__ __forceinline__ float word_to_float(unsigned l, float scale) {
+  const float fa = __uint_as_float(0x4B000000u | (l >> 23)) - 8388608.f;
+  const float fb = __uint_as_float(0x4B000000u | (l & 0x7fffffu)) - 8388608.f;
+  return fmaf(fa, 8388608.f, fb) * scale;
+}
+
+// The float of a cell's sum: low word l (and, for two-word tiles, coarse word c).
+__device__ __forceinline__ float sum_to_float(const TileSum& t, unsigned l, unsigned c) {
+  return t.s ? word_to_float(l, t.ms) : fixed_to_float(l, c, t.ms);
 }
 
 // Adds the 8 quantised weights q of a particle with base cell (cx, ly, lz) (ly, lz relative
 // to the tile, in [-1, TY-1] x [-1, TZ-1]) to the tile accumulators; tile row r of lo / hi
 // starts at word r * rs.  Corners outside the tile's rows are skipped (a neighbouring tile
-// adds them), unless the whole particle is inside.
+// adds them), unless the whole particle is inside.  ONE: one-word sums (lo only).
+template <bool ONE>
 __device__ __forceinline__ void deposit_particle(unsigned* lo, unsigned* hi, int n, int rs, int cx, int ly, int lz,
                                                  const unsigned (&q)[8]) {
   const int x1 = cx + 1 == n ? 0 : cx + 1;
@@ -40,28 +86,32 @@ __device__ __forceinline__ void deposit_particle(unsigned* lo, unsigned* hi, int
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     const int ty2 = ly + corner_y(k), tz2 = lz + corner_z(k);
-    if (inside || (ty2 >= 0 && ty2 < TY && tz2 >= 0 && tz2 < TZ))
-      acc_add(lo, hi, base + (corner_z(k) * TY + corner_y(k)) * rs + (corner_x(k) ? x1 : cx), q[k]);
+    if (inside || (ty2 >= 0 && ty2 < TY && tz2 >= 0 && tz2 < TZ)) {
+      const int i = base + (corner_z(k) * TY + corner_y(k)) * rs + (corner_x(k) ? x1 : cx);
+      if (ONE) atomicAdd(&lo[i], q[k]);  // result unused: a non-returning shared-memory reduction
+      else acc_add(lo, hi, i, q[k]);
+    }
   }
 }
 
-// Quantised CIC weights (2^-26) of a particle.
-__device__ __forceinline__ void quantised_weights(const Cell& c, unsigned (&q)[8]) {
+// CIC weights of a particle quantised to qscale = 2^s.
+__device__ __forceinline__ void quantised_weights(const Cell& c, float qscale, unsigned (&q)[8]) {
   float wt[8];
   cic_weights(c, wt);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) q[k] = __float2uint_rn(wt[k] * (float)(1u << PM_FIX_BITS));
+  for (int k = 0; k < 8; ++k) q[k] = __float2uint_rn(wt[k] * qscale);
 }
 
 // (Pre-adding the weights of lanes that share a cell, with __match_any_sync and a warp
 // reduction, would cut the same-address atomics of clustered tiles, but the match alone made
 // the deposit 6x slower on GB300.)
-__device__ __forceinline__ void deposit_entry(unsigned* lo, unsigned* hi, int n, int rs, bool ok, const Cell& c,
-                                              int ly, int lz) {
+template <bool ONE>
+__device__ __forceinline__ void deposit_entry(unsigned* lo, unsigned* hi, int n, int rs, float qscale, bool ok,
+                                              const Cell& c, int ly, int lz) {
   if (ok) {
     unsigned q[8];
-    quantised_weights(c, q);
-    deposit_particle(lo, hi, n, rs, c.x, ly, lz, q);
+    quantised_weights(c, qscale, q);
+    deposit_particle<ONE>(lo, hi, n, rs, c.x, ly, lz, q);
   }
 }
 
@@ -147,25 +197,16 @@ __device__ __forceinline__ void run_table(const RunLoad& v, int lane, unsigned* 
   if (lane == 0) s_off[0] = 0;
 }
 
-// Accumulate the tile at (y0, z0) of simulation S into lo/hi (TZ * TY rows of n cells,
-// row r at word r * rs of each; lo and hi together are 2 * TZ * TY * n contiguous words).
-// s_begin / s_off: NRUN + 1 words each, already holding the tile's run table when
-// runs_ready.  Entered and left by all NT threads, synchronised.
-template <int MODE, int NT>
-__device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
-                                             const unsigned* __restrict__ row_start, int* err, int y0, int z0,
-                                             unsigned* lo, unsigned* hi, int rs, unsigned* s_begin, unsigned* s_off,
-                                             bool runs_ready = false) {
+// The particle loop of a tile: two source entries per lane and iteration, so that their
+// loads overlap; the slots (the permutation entries) of the next iteration are in flight
+// while this one adds its particles.
+template <int MODE, int NT, bool ONE>
+__device__ __forceinline__ void deposit_sources(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
+                                                int* err, int y0, int z0, unsigned* lo, unsigned* hi, int rs,
+                                                const unsigned* s_begin, const unsigned* s_off, unsigned total,
+                                                float qscale) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n = S.n;
-  const int ncell = TZ * TY * n;  // zero 2 * ncell words
-  uint4* z4 = reinterpret_cast<uint4*>(lo);
-  for (int i = threadIdx.x; i < ncell / 2; i += NT) z4[i] = make_uint4(0u, 0u, 0u, 0u);
-  if (warp == 0 && !runs_ready) run_table(run_load(S, row_start, y0, z0, lane), lane, s_begin, s_off);
-  __syncthreads();
-  const unsigned total = s_off[NRUN];
-  // two source entries per lane and iteration, so that their loads overlap; the slots (the
-  // permutation entries) of the next iteration are in flight while this one adds its particles
   unsigned base = (unsigned)warp * 32u;
   unsigned sl0 = source_slot(perm, s_begin, s_off, base + lane, total);
   unsigned sl1 = source_slot(perm, s_begin, s_off, base + NT + lane, total);
@@ -177,10 +218,45 @@ __device__ __forceinline__ void deposit_tile(const Sim& S, const Parts& p, const
     int ly0 = 0, lz0 = 0, ly1 = 0, lz1 = 0;
     const bool ok0 = source_cell<MODE>(S, p, q0, y0, z0, err, c0, ly0, lz0);
     const bool ok1 = source_cell<MODE>(S, p, q1, y0, z0, err, c1, ly1, lz1);
-    deposit_entry(lo, hi, n, rs, ok0, c0, ly0, lz0);
-    deposit_entry(lo, hi, n, rs, ok1, c1, ly1, lz1);
+    deposit_entry<ONE>(lo, hi, n, rs, qscale, ok0, c0, ly0, lz0);
+    deposit_entry<ONE>(lo, hi, n, rs, qscale, ok1, c1, ly1, lz1);
+  }
+}
+
+// Accumulate the tile at (y0, z0) of simulation S into lo/hi: TZ * TY rows of n cells, row r
+// of lo at word r * rs and of hi at the same offset from hi (hi is only written by two-word
+// tiles).  s_begin / s_off: NRUN + 1 words each, already holding the tile's run table when
+// runs_ready.  Entered and left by all NT threads, synchronised.  Returns how the sums are
+// held (tile_sum).
+template <int MODE, int NT>
+__device__ __forceinline__ TileSum deposit_tile(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
+                                                const unsigned* __restrict__ row_start, int* err, int y0, int z0,
+                                                unsigned* lo, unsigned* hi, int rs, unsigned* s_begin,
+                                                unsigned* s_off, bool runs_ready = false) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n = S.n;
+  if (!runs_ready) {
+    if (warp == 0) run_table(run_load(S, row_start, y0, z0, lane), lane, s_begin, s_off);
+    __syncthreads();
+  }
+  const unsigned total = s_off[NRUN];
+  const TileSum ts = tile_sum(total, S.mass_scale);
+  // zero the rows of lo (and of hi for two-word sums), 4 words per store
+  const int q4 = n / 4;
+  for (int i = threadIdx.x; i < TZ * TY * q4; i += NT) {
+    const int off = (i / q4) * rs + (i % q4) * 4;
+    *reinterpret_cast<uint4*>(lo + off) = make_uint4(0u, 0u, 0u, 0u);
+    if (!ts.s) *reinterpret_cast<uint4*>(hi + off) = make_uint4(0u, 0u, 0u, 0u);
   }
   __syncthreads();
+  if (ts.s)
+    deposit_sources<MODE, NT, true>(S, p, perm, err, y0, z0, lo, hi, rs, s_begin, s_off, total,
+                                    __uint_as_float((unsigned)(127 + ts.s) << 23));
+  else
+    deposit_sources<MODE, NT, false>(S, p, perm, err, y0, z0, lo, hi, rs, s_begin, s_off, total,
+                                     (float)(1u << PM_FIX_BITS));
+  __syncthreads();
+  return ts;
 }
 
 }  // namespace pm

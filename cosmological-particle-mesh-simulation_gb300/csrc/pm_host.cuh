@@ -38,6 +38,12 @@ struct DBuf {
     if (e == cudaSuccess) bytes = b;
     return e;
   }
+  // as ensure, but growing to at least 3/2 of the current size: fewer reallocations (and so
+  // fewer cudaFree calls, each of which synchronises the device) for sizes that creep up
+  cudaError_t ensure_geo(size_t b) {
+    if (b <= bytes && p) return cudaSuccess;
+    return ensure(b > bytes + bytes / 2 ? b : bytes + bytes / 2);
+  }
   void release() {
     if (p) cudaFree(p);
     p = nullptr;

@@ -1,12 +1,12 @@
 // pm_density_noalloc: the CIC deposit for callers that cannot allocate device memory.
 //
 // Some callers of this library may not call cudaMalloc at all:
-// * code that runs while a CUDA stream is being captured into a graph (allocation is not
-//   a capturable operation);
-// * hosts whose device memory is carved up by a pool or arena up front, where a library
-//   that allocates on its own breaks the budget;
-// * latency-critical loops where an allocation (and the device synchronisation that
-//   cudaMalloc/cudaFree can imply) is not acceptable.
+// * hosts whose device memory is carved up up front by a pool or an arena (a framework's
+//   caching allocator, a fixed budget per tenant): a library that allocates on its own
+//   either fails there or breaks the host's accounting;
+// * latency-critical loops, where an allocation and the device-wide synchronisation that
+//   cudaMalloc / cudaFree can imply are not acceptable;
+// * plugin hosts that hand every buffer to their plugins and forbid them to allocate.
 // For them this entry point keeps every piece of scratch memory it needs -- the
 // simulation descriptor, the work table, the sort's key/value buffers and histograms,
 // the x-row starts -- in one file-scope static device array of fixed size.  Every GPU
@@ -16,10 +16,16 @@
 // cells per side.  Larger requests are rejected with PM_ERR_ARG; pm_density, which
 // allocates, has no such limit.
 //
+// The first call on a device does a one-time set-up with that device current: it looks up
+// the array's device address (cudaGetSymbolAddress) and sets the kernels' attributes.
+// The set-up is thread-safe (one lock per process).  Make that first call before any
+// stream capture.
+//
 // The array is shared by every call: two calls whose work overlaps on the GPU (different
 // streams, or different host threads, without ordering between them) race on it.  Each
-// call writes all the scratch it reads before reading it, and clears the device check
-// word it uses, so one call never sees stale data from the one before.
+// call writes all the scratch it reads before reading it -- the descriptor and the work
+// table come from a kernel that receives them as arguments, which also clears the device
+// check word -- so one call never sees stale data from the one before.
 #include "pm_host.cuh"
 
 using namespace pm;
@@ -30,7 +36,6 @@ constexpr long long NOALLOC_MAX_PARTICLES = 1ll << 18;  // 262,144 particles (64
 constexpr int NOALLOC_MAX_N = 128;                      // grid cells per side
 constexpr long long NOALLOC_MAX_ROWS = (long long)NOALLOC_MAX_N * NOALLOC_MAX_N;
 constexpr int NOALLOC_MAX_BLOCKS = (int)((NOALLOC_MAX_PARTICLES + SORT_TILE - 1) / SORT_TILE);
-constexpr int MAX_DEVICES = 64;
 
 struct NoAllocScratch {
   Sim sim;
@@ -52,18 +57,39 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocS
 // Device address of g_noalloc_scratch per device, found once per device by the first call.
 // In host code the array's name only stands for the symbol: its device address must come
 // from cudaGetSymbolAddress with that device current.
-NoAllocScratch* g_scratch_ptr[MAX_DEVICES] = {};
+std::atomic<NoAllocScratch*> g_scratch_ptr[PM_MAX_DEVICES];
+std::mutex g_setup_lock;
 
 int setup(int device, NoAllocScratch** out) {
-  if (device < 0 || device >= MAX_DEVICES) return PM_ERR_ARG;
-  if (!g_scratch_ptr[device]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return PM_ERR_CUDA;
-    if (deposit_prepare() != cudaSuccess) return PM_ERR_CUDA;
-    g_scratch_ptr[device] = static_cast<NoAllocScratch*>(p);
+  if (device < 0 || device >= PM_MAX_DEVICES) return PM_ERR_ARG;
+  NoAllocScratch* p = g_scratch_ptr[device].load(std::memory_order_acquire);
+  if (!p) {
+    std::lock_guard<std::mutex> g(g_setup_lock);
+    p = g_scratch_ptr[device].load(std::memory_order_relaxed);
+    if (!p) {
+      void* a = nullptr;
+      if (cudaGetSymbolAddress(&a, g_noalloc_scratch) != cudaSuccess || !a) return PM_ERR_CUDA;
+      if (deposit_prepare() != cudaSuccess || sort_prepare() != cudaSuccess) return PM_ERR_CUDA;
+      p = static_cast<NoAllocScratch*>(a);
+      g_scratch_ptr[device].store(p, std::memory_order_release);
+    }
   }
-  *out = g_scratch_ptr[device];
+  *out = p;
   return PM_OK;
+}
+
+// Writes the call's descriptor and work table into the scratch and clears its check word.
+// They arrive as kernel arguments, which the launch copies: nothing is read from host
+// memory after this call has returned.
+__global__ void k_noalloc_begin(NoAllocScratch* s, Sim sim, int key_units, int dep_units) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    s->sim = sim;
+    s->prefix[0] = 0;
+    s->prefix[1] = key_units;
+    s->prefix[2] = 0;
+    s->prefix[3] = dep_units;
+    s->err = 0;
+  }
 }
 
 }  // namespace
@@ -79,11 +105,7 @@ extern "C" int pm_density_noalloc(const float* positions, long long np, int n_ce
   if (int r = setup(device, &s)) return r;
   cudaStream_t st = (cudaStream_t)stream;
 
-  struct {
-    Sim sim;
-    int prefix[6];
-  } host{};
-  Sim& d = host.sim;
+  Sim d{};
   d.n = n_cells;
   d.pitch = spec_pitch(n_cells);
   d.xbits = ceil_log2(n_cells);
@@ -94,12 +116,8 @@ extern "C" int pm_density_noalloc(const float* positions, long long np, int n_ce
   d.mass_scale = (float)(mass / (double)(1u << PM_FIX_BITS));
   const int key_units = (int)((np + 255) / 256);
   const int dep_units = (n_cells / TILE_Y) * (n_cells / TILE_Z);
-  host.prefix[0] = 0;
-  host.prefix[1] = key_units;
-  host.prefix[2] = 0;
-  host.prefix[3] = dep_units;
-  if (cudaMemcpyAsync(s, &host, sizeof(host), cudaMemcpyHostToDevice, st) != cudaSuccess) return PM_ERR_CUDA;
-  if (cudaMemsetAsync(&s->err, 0, sizeof(int), st) != cudaSuccess) return PM_ERR_CUDA;
+  k_noalloc_begin<<<1, 32, 0, st>>>(s, d, key_units, dep_units);
+  if (cudaGetLastError() != cudaSuccess) return PM_ERR_CUDA;
 
   Parts p{};
   p.x = const_cast<float*>(positions);
@@ -107,8 +125,7 @@ extern "C" int pm_density_noalloc(const float* positions, long long np, int n_ce
   p.z = p.x + 2 * np;
   Work wk{s->prefix + 0, 1, key_units};
   Work wd{s->prefix + 2, 1, dep_units};
-  int sms = 0;
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return PM_ERR_CUDA;
+  const int sms = device_sms();
   if (launch_keys_abs(&s->sim, wk, p, s->keys, nullptr, &s->err, grid_for(key_units, sms, 16), st))
     return PM_ERR_CUDA;
   SortScratch ss;

@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(KEY_NT) k_keys(const Sim* __restrict__ sims, W
     const Sim& S = sims[si];
     const long long i = (long long)(unit - __ldg(&w.prefix[si])) * KEY_NT + threadIdx.x;
     if (i >= S.np) continue;
-    const long long slot = S.part_off + i;
+    const long long slot = S.slot_off + i;
     // from the state itself (the cell records, if any, are written here)
     Cell c;
     if (MODE == POS_ABS) {
@@ -90,16 +90,15 @@ __global__ void __launch_bounds__(DEP_NT, 3) k_deposit(const Sim* __restrict__ s
     const int y0 = (local % ntile_y) * TY, z0 = (local / ntile_y) * TZ;
     unsigned* lo = reinterpret_cast<unsigned*>(acc_raw);
     unsigned* hi = lo + TZ * TY * n;
-    deposit_tile<MODE, DEP_NT>(S, p, perm, row_start, err, y0, z0, lo, hi, S.n, s_begin, s_off);
-    const float ms = S.mass_scale;
+    const TileSum ts = deposit_tile<MODE, DEP_NT>(S, p, perm, row_start, err, y0, z0, lo, hi, S.n, s_begin, s_off);
     for (int row = warp; row < TZ * TY; row += DEP_NT / 32) {
       const uint4* l4 = reinterpret_cast<const uint4*>(lo + row * n);
       const uint4* h4 = reinterpret_cast<const uint4*>(hi + row * n);
       float4* dst = reinterpret_cast<float4*>(S.rho + ((long long)(z0 + row / TY) * n + (y0 + row % TY)) * n);
       for (int x4 = lane; x4 < n / 4; x4 += 32) {
-        const uint4 l = l4[x4], h = h4[x4];
-        dst[x4] = make_float4(fixed_to_float(l.x, h.x, ms), fixed_to_float(l.y, h.y, ms),
-                              fixed_to_float(l.z, h.z, ms), fixed_to_float(l.w, h.w, ms));
+        const uint4 l = l4[x4], h = ts.s ? make_uint4(0u, 0u, 0u, 0u) : h4[x4];
+        dst[x4] = make_float4(sum_to_float(ts, l.x, h.x), sum_to_float(ts, l.y, h.y), sum_to_float(ts, l.z, h.z),
+                              sum_to_float(ts, l.w, h.w));
       }
     }
     __syncthreads();
@@ -382,6 +381,8 @@ cudaError_t launch_disp_to_abs(Parts in, long long off, long long np, int np1, i
 }
 
 cudaError_t deposit_prepare() {
+  static DeviceOnce once;
+  return once.run([]() {
   cudaError_t e = cudaFuncSetAttribute(k_deposit<POS_ABS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)deposit_smem_bytes(PM_MAX_N, 4, 4));
   if (!e) e = cudaFuncSetAttribute(k_deposit<POS_DISP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -389,6 +390,7 @@ cudaError_t deposit_prepare() {
   if (!e) e = cudaFuncSetAttribute(k_deposit<POS_ABS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (!e) e = cudaFuncSetAttribute(k_deposit<POS_DISP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   return e;
+  });
 }
 
 size_t deposit_smem_bytes(int n, int ty, int tz) { return (size_t)n * ty * tz * sizeof(unsigned long long); }
@@ -449,12 +451,7 @@ cudaError_t launch_tile_order(const Sim* sims, const Work& w, const unsigned* ro
 cudaError_t launch_deposit(const Sim* sims, const Work& w, Parts p, const unsigned* perm,
                            const unsigned* row_start, int mode, int* err, int ctas, size_t smem,
                            cudaStream_t st) {
-  static bool init = false;
-  if (!init) {
-    cudaError_t e = deposit_prepare();
-    if (e) return e;
-    init = true;
-  }
+  if (cudaError_t e = deposit_prepare()) return e;
   if (mode == POS_ABS) k_deposit<POS_ABS><<<ctas, DEP_NT, smem, st>>>(sims, w, p, perm, row_start, err);
   else k_deposit<POS_DISP><<<ctas, DEP_NT, smem, st>>>(sims, w, p, perm, row_start, err);
   return cudaGetLastError();

@@ -214,6 +214,13 @@ size_t sort_scratch_hist_entries(long long n) {
   return (size_t)MAX_RADIX * (nb > 0 ? nb : 1);
 }
 
+cudaError_t sort_prepare() {
+  static DeviceOnce once;
+  return once.run([]() {
+    return cudaFuncSetAttribute(k_sort_downsweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(DownSmem));
+  });
+}
+
 int radix_sort_passes(int bits) { return bits <= 0 ? 1 : (bits + MAX_DIGIT_BITS - 1) / MAX_DIGIT_BITS; }
 
 cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int begin_bit, int bits, bool gen_vals,
@@ -223,13 +230,7 @@ cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int begin_bi
   if (n > s.capacity || n >= (1ll << 32)) return cudaErrorInvalidValue;
   const int nblocks = (int)((n + SORT_TILE - 1) / SORT_TILE);
   if (nblocks > s.max_blocks) return cudaErrorInvalidValue;
-  static bool init = false;
-  if (!init) {
-    cudaError_t e = cudaFuncSetAttribute(k_sort_downsweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(DownSmem));
-    if (e) return e;
-    init = true;
-  }
+  if (cudaError_t e = sort_prepare()) return e;
   const int passes = radix_sort_passes(bits);
   const int dbits = bits <= 0 ? 1 : (bits + passes - 1) / passes;
   unsigned *ki = keys, *vi = vals, *ko = s.keys_alt, *vo = s.vals_alt;
@@ -258,7 +259,8 @@ cudaError_t radix_sort(unsigned* keys, unsigned* vals, long long n, int begin_bi
 // radix passes.  The order inside a row depends on the scheduling of the cursor atomics;
 // nothing downstream depends on it (the deposit sums integers, the kick is per particle).
 // Equal keys of a warp are combined by a match first (the state is nearly sorted, so a
-// warp touches few rows).
+// warp touches few rows).  A key 0xffffffff marks an empty slot (a simulation that left a
+// batch): it is neither counted nor placed.
 // ---------------------------------------------------------------------------------
 namespace {
 
@@ -279,7 +281,7 @@ __global__ void __launch_bounds__(CS_NT) k_row_hist(const unsigned* __restrict__
     for (int u = 0; u < CS_UNR; ++u) {
       const long long i = b + u * 32 + lane;
       k[u] = i < n ? __ldg(&keys[i]) : 0xffffffffu;
-      if (i < n && k[u] >= nrows) {
+      if (k[u] != 0xffffffffu && k[u] >= nrows) {
         set_error(err, ERR_CELL_RANGE);
         k[u] = nrows - 1;
       }
@@ -373,7 +375,7 @@ __global__ void __launch_bounds__(CS_NT) k_row_scatter(const unsigned* __restric
       for (int u = 0; u < CS_UNR; ++u) {
         const long long i = b + u * 32 + lane;
         k[u] = i < end ? __ldg(&keys[i]) : 0xffffffffu;
-        if (i < end && k[u] >= nrows) k[u] = nrows - 1;
+        if (k[u] != 0xffffffffu && k[u] >= nrows) k[u] = nrows - 1;
       }
 #pragma unroll
       for (int u = 0; u < CS_UNR; ++u) {

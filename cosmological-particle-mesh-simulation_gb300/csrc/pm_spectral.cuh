@@ -629,17 +629,6 @@ inline bool encode_spectrum_map(CUtensorMap* tm, const void* spec, int n, bool z
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-inline int device_sms() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
-  }
-  return sms;
-}
-
 // ---------------------------------------------------------------------------------
 // x passes fed by bulk copies, one simulation per launch.
 //
@@ -799,9 +788,9 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
     const Sim& S = sims[si];
     const int local = unit - __ldg(&w.prefix[si]);
     const int y0 = (local % (N / TY)) * TY, z0 = (local / (N / TY)) * TZ;
-    deposit_tile<MODE, NT>(S, p, perm, row_start, err, y0, z0, lo, hi, RS, s_begin, s_off, runs_ready);
+    const TileSum ts = deposit_tile<MODE, NT>(S, p, perm, row_start, err, y0, z0, lo, hi, RS, s_begin, s_off,
+                                              runs_ready);
     runs_ready = false;
-    const float ms = S.mass_scale;
     if constexpr (xrow_ok(N)) {
       // the tile's NL rows: T lanes per row, rows r = warp * RPW + sub; the row's exchange
       // buffer overlays its own accumulator words once they are read
@@ -821,8 +810,8 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
 #pragma unroll
           for (int a = 0; a < P; ++a) {
             const int j = Q * a + t + T * i;  // z[j] = x[2j] + i x[2j+1]
-            const uint2 ll = l2[j], hh = h2[j];
-            v2[i][a] = make_float2(fixed_to_float(ll.x, hh.x, ms), fixed_to_float(ll.y, hh.y, ms));
+            const uint2 ll = l2[j], hh = ts.s ? make_uint2(0u, 0u) : h2[j];
+            v2[i][a] = make_float2(sum_to_float(ts, ll.x, hh.x), sum_to_float(ts, ll.y, hh.y));
           }
         // warp 0 takes the next tile and loads its run table now, and stores it after the
         // transform, so that the loads' latency hides behind it (the table is free: the
@@ -854,7 +843,7 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       const int i = threadIdx.x + k * NT;
-      v[k] = fixed_to_float(lo[i], hi[i], ms);
+      v[k] = sum_to_float(ts, lo[i], ts.s ? 0u : hi[i]);
     }
     __syncthreads();
 #pragma unroll
@@ -889,16 +878,16 @@ cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned*
   if constexpr (!deposit_r2c_ok(N)) {
     return cudaErrorNotSupported;
   } else {
-  static bool init = false;
+  static DeviceOnce once;
   const size_t sm = deposit_r2c_smem_bytes(N);
-  if (!init) {
+  const cudaError_t ie = once.run([&]() {
     cudaError_t e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_ABS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (!e) e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_DISP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (!e) e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_ABS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (!e) e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_DISP>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    if (e) return e;
-    init = true;
-  }
+    return e;
+  });
+  if (ie) return ie;
   if (ctas <= 0) return cudaSuccess;  // attribute setup only
   constexpr int NT = deposit_r2c_nt(N);
   if (next_tile) {
@@ -923,9 +912,9 @@ static cudaError_t max_shared(K kern, size_t bytes) {
 template <int N>
 cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cudaStream_t st,
                             const CUtensorMap* maps, int* err) {
-  static bool init = false;
+  static DeviceOnce once;
   const size_t xs = x_smem_bytes(N), ls = line_smem_bytes(N);
-  if (!init) {
+  const cudaError_t ie = once.run([&]() -> cudaError_t {
     if constexpr (tma_rows(N)) {
       cudaError_t e = max_shared(k_x_tma<N, false>, xtma_smem_bytes(N));
       if (!e) e = max_shared(k_x_tma<N, true>, xtma_smem_bytes(N));
@@ -948,9 +937,9 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
     if (!e) e = max_shared(k_line_pass<N, true, true>, ls);
     if (!e) e = max_shared(k_z_green<N, false>, ls);
     if (!e) e = max_shared(k_z_green<N, true>, ls);
-    if (e) return e;
-    init = true;
-  }
+    return e;
+  });
+  if (ie) return ie;
   if (kind == SPEC_PREPARE) return cudaSuccess;
   const int grid = w.total < device_sms() ? w.total : device_sms();
   if constexpr (xrow_ok(N)) {

@@ -7,7 +7,7 @@ engine: CUDA graphs, fused kernels); RESIDENT = False runs the reference's loop 
 from time import time
 
 from configure_me import (A_END, A_INIT, BOX_SIZE, H0, N_CELLS, N_PARTS, N_SAVE_FILES, OMEGA_M0,
-                          PRINT_STATUS, RESTART, RESTART_FROM_N, SAVE_DATA, STEPS)
+                          PRINT_STATUS, RESTART, RESTART_FROM_N, SAVE_DATA, SAVE_DENSITY, STEPS)
 import configure_me
 from density import density
 from fourier_utils import fourier_grid
@@ -56,10 +56,12 @@ def simulator():
 
 def _resident(positions, velocities, a_current, da, da_save, n_file):
     from pmgpu.batch import Batch
+    from pmgpu.config import step_count
     from pmgpu.dropin import config
     cfg = config()
     cfg.a_init = float(a_current)
     cfg.steps = max(1, int(round((A_END - a_current) / da)))
+    nsteps = step_count(cfg.a_init, cfg.a_end, cfg.steps)
     b = Batch()
     sid = b.add(cfg, positions, velocities)
     writer = None
@@ -68,17 +70,27 @@ def _resident(positions, velocities, a_current, da, da_save, n_file):
         from save_data import DATA_DIR
         writer = SnapshotWriter(BOX_SIZE, N_CELLS, H0, directory=DATA_DIR)
     print("Starting the integrations (resident on the GPU)...")
-    while b.active(sid):
+    while True:
+        a, done = b.state(sid)
+        if done >= nsteps:
+            break
         start_time = time()
         # run up to the next snapshot boundary in one call
-        a, done = b.state(sid)
         target = A_INIT + n_file * da_save
-        k = max(1, int((target - a) / da)) if SAVE_DATA else cfg.steps
-        b.step(k)
+        k = min(max(1, int((target - a) / da)) if SAVE_DATA else nsteps, nsteps - done)
+        rho = None
+        if SAVE_DATA and SAVE_DENSITY:
+            # pmesh.py:60-67 saves the density the interval's last step was computed from
+            if k > 1:
+                b.step(k - 1)
+            rho = b.density(sid)
+            b.step(1)
+        else:
+            b.step(k)
         a, done = b.state(sid)
         if SAVE_DATA and a >= target:
             pos_d, vel_d, _, _ = b.get(sid, device=True)
-            writer.submit(n_file, pos_d, vel_d, a)
+            writer.submit(n_file, pos_d, vel_d, a, rho=rho)
             n_file += 1
         if PRINT_STATUS:
             print_status(a, start_time)

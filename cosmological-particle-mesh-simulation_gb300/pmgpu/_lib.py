@@ -67,11 +67,13 @@ SIGNATURES = {
     "pm_batch_step": (c_int, [c_void_p, c_int, c_void_p]),
     "pm_batch_get": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, P_double, P_int, c_void_p]),
     "pm_batch_active": (c_int, [c_void_p, c_int]),
+    "pm_batch_density": (c_int, [c_void_p, c_int, c_void_p, c_void_p]),
     "pm_batch_remove": (c_int, [c_void_p, c_int]),
     "pm_batch_set_graphs": (c_int, [c_void_p, c_int]),
     "pm_batch_check": (c_int, [c_void_p, c_void_p, P_int]),
     "pm_batch_profile": (c_int, [c_void_p, c_int, ctypes.POINTER(ctypes.c_float), c_int, c_void_p]),
     "pm_batch_launches_per_step": (c_int, [c_void_p]),
+    "pm_batch_host_seconds": (c_int, [c_void_p, P_double, c_int]),
 }
 PROFILE_PHASES = ("sort", "rows", "deposit", "x_r2c", "y_fwd", "z_green", "y_inv", "x_c2r", "kick", "coef")
 

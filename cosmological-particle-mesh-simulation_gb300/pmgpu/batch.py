@@ -71,6 +71,12 @@ class Batch:
         stream = torch.cuda.current_stream().cuda_stream
         self._check(self._lib.pm_batch_step(self._h, int(nsteps), ctypes.c_void_p(stream)))
 
+    def mark(self):
+        """A CUDA event recorded after the work enqueued so far (on the current stream)."""
+        ev = torch.cuda.Event()
+        ev.record()
+        return ev
+
     def active(self, sid: int) -> bool:
         r = self._lib.pm_batch_active(self._h, sid)
         if r < 0:
@@ -97,6 +103,15 @@ class Batch:
                                                ctypes.byref(done), stream))
         return pos, vel, a.value, done.value
 
+    def density(self, sid: int, out=None):
+        """CIC density (N_CELLS^3 float32 CUDA tensor) of a resident simulation's current state."""
+        n = self.cfgs[sid].n_cells
+        if out is None:
+            out = torch.empty((n, n, n), dtype=torch.float32, device=f"cuda:{self.device}")
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self._check(self._lib.pm_batch_density(self._h, sid, ctypes.c_void_p(out.data_ptr()), stream))
+        return out
+
     def state(self, sid: int):
         a = ctypes.c_double(0)
         done = ctypes.c_int(0)
@@ -114,6 +129,12 @@ class Batch:
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         self._check(self._lib.pm_batch_profile(self._h, int(nsteps), arr, len(arr), stream))
         return dict(zip(_lib.PROFILE_PHASES, [float(x) for x in arr]))
+
+    def host_seconds(self) -> dict:
+        """Host time spent so far in admissions, planning, graph capture and retirements."""
+        arr = (ctypes.c_double * 4)()
+        self._check(self._lib.pm_batch_host_seconds(self._h, arr, 4))
+        return dict(zip(("admit", "plan", "capture", "retire"), [round(float(x), 4) for x in arr]))
 
     def launches_per_step(self) -> int:
         return int(self._lib.pm_batch_launches_per_step(self._h))

@@ -6,9 +6,12 @@ of the reference's rejection loop (device_ics=True, the default; the Gaussian fi
 Zel'dovich step then run on the GPU at admission, milliseconds) or the whole initial
 conditions (device_ics=False).  Once they are ready and its footprint fits under the
 memory cap, it joins the resident batch (continuous batching: requests that arrive while
-others run are admitted as slots and memory free up).  The batch advances all resident simulations together, a few steps per tick; a
-finished simulation leaves the batch at once and its memory admits the next request.
-Latency = completion time - arrival time (initial conditions, queueing and stepping).
+others run are admitted as slots and memory free up).  The batch advances all resident
+simulations together, a few steps per tick; the host enqueues at most `ahead` ticks beyond
+what the device has finished, so that admissions wait little.  A finished simulation leaves
+the batch at once (no copy of the others' state) and its memory admits the next request.
+Latency = completion time - arrival time (initial conditions, queueing and stepping), with
+completion observed when the simulation's final state is complete on the device.
 """
 from __future__ import annotations
 
@@ -90,7 +93,7 @@ class Server:
     """Runs a request stream against one GPU in real time."""
 
     def __init__(self, mem_cap_bytes: int, ic_workers: int = 8, steps_per_tick: int = 4, device: int = 0,
-                 keep_results: bool = False, device_ics: bool = True, pk: bool = False):
+                 keep_results: bool = False, device_ics: bool = True, pk: bool = False, ahead: int = 2):
         import torch
         from .batch import Batch
         self.batch = Batch(device=device, mem_cap_bytes=mem_cap_bytes)
@@ -105,6 +108,11 @@ class Server:
         self.pool = cf.ProcessPoolExecutor(max_workers=ic_workers, mp_context=mp.get_context("spawn"))
         self.keep_results = keep_results
         self.outputs = {}
+        self.ahead = max(1, ahead)
+
+    def host_seconds(self) -> dict:
+        """Host time the batch engine spent in admissions, planning, graph capture, retirements."""
+        return self.batch.host_seconds()
 
     def close(self):
         self.pool.shutdown(wait=False, cancel_futures=True)
@@ -136,6 +144,9 @@ class Server:
 
     def run(self, stream: list[Request], time_limit: float | None = None) -> list[Result]:
         from .batch import Batch
+        ticks = []  # events of the ticks enqueued and not yet known to be finished
+        mark = getattr(self.batch, "mark", None)
+        ahead = getattr(self, "ahead", 2)
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0  # noqa: E731
         pending = sorted(stream, key=lambda r: r.arrival)
@@ -179,7 +190,11 @@ class Server:
                 queued.pop(0)
                 active[sid] = (r, now())
             if active:
+                while len(ticks) >= ahead:  # bound the work enqueued beyond the device
+                    ticks.pop(0).synchronize()
                 self.batch.step(self.steps_per_tick)
+                if mark is not None:
+                    ticks.append(mark())
                 for sid in list(active):
                     if not self.batch.active(sid):
                         r, ta = active.pop(sid)

@@ -124,14 +124,20 @@ int pm_project(pm_ctx* ctx, const float* rho, int n_slices, double* out, void* s
 int pm_power_spectrum(pm_ctx* ctx, const float* rho, double box_size, int nbins, double* k_out,
                       double* pk_out, double* modes_out, void* stream);
 
-/* The CIC deposit of pm_density for callers that cannot allocate device memory (code
-   running during stream capture, memory carved up by an arena, latency-critical loops).
-   No counterpart in the reference.  All scratch lives in one static device array of the
-   library (about 4.3 MB per GPU, held until the process exits): at most 262,144
-   particles and n_cells <= 128, otherwise PM_ERR_ARG.  Calls no allocating routine.  The
-   first call on a device looks up the array's address (cudaGetSymbolAddress) and sets
-   kernel attributes: make it before any stream capture.  Calls share the array, so calls
-   that overlap on the GPU race; invalid particles are skipped without a report. */
+/* The CIC deposit of pm_density for callers that cannot allocate device memory: hosts whose
+   device memory is carved up up front by a pool or an arena (a library that allocates on
+   its own fails there or breaks the host's accounting), latency-critical loops that cannot
+   take the synchronisation cudaMalloc / cudaFree can imply, plugin hosts that hand every
+   buffer to their plugins.  No counterpart in the reference.  The caller passes the
+   positions and the density grid; all scratch lives in one static device array of the
+   library (about 4.3 MB per GPU that loads the library, held until the process exits).
+   Limits: at most 262,144 particles and n_cells <= 128; larger requests return PM_ERR_ARG
+   and do nothing.  Calls no cudaMalloc, cudaFree or other allocating routine.  The first
+   call on a device sets up (with that device current, thread-safe): it looks up the array's
+   device address with cudaGetSymbolAddress and sets kernel attributes; make that first call
+   before any stream capture.  Every call shares the array and rewrites all of it that it
+   reads, so calls that overlap on the GPU race; particles with non-finite or off-grid
+   coordinates are skipped without a report. */
 int pm_density_noalloc(const float* positions, long long np, int n_cells, double mass, float* rho,
                        void* stream);
 
@@ -169,18 +175,28 @@ const char* pm_batch_last_error(const pm_batch* b);
 /* Device bytes a simulation of this configuration holds while resident. */
 size_t pm_sim_footprint(const pm_config* cfg);
 /* Admits a simulation from absolute positions/velocities (3, N_PARTS^3) at cfg->a_init;
-   on_device selects device or host input arrays.  PM_ERR_ADMIT if over the cap. */
+   on_device selects device or host input arrays (device arrays must be complete: work that
+   writes them on another stream has finished).  The arrays are no longer used when this
+   returns.  It waits for the steps already enqueued, not for the device as a whole.
+   PM_ERR_ADMIT if over the cap. */
 int pm_batch_add(pm_batch* b, const pm_config* cfg, const float* positions,
                  const float* velocities, int on_device, int* sim_id);
 /* 1 if pm_batch_add of this configuration would pass the memory cap now, else 0. */
 int pm_batch_admits(pm_batch* b, const pm_config* cfg);
 /* Advances every active simulation by up to nsteps steps (a simulation stops after the
-   src/pmesh.py:56 loop count).  Work is enqueued on `stream` (CUDA graphs). */
+   src/pmesh.py:56 loop count).  Work is enqueued on `stream` (CUDA graphs); with a NULL
+   stream the call returns after the work has finished.  A simulation that has run its last
+   step leaves the batch (its final state is extracted on `stream`). */
 int pm_batch_step(pm_batch* b, int nsteps, void* stream);
 /* Copies a simulation's state out (absolute positions in particle order). */
 int pm_batch_get(pm_batch* b, int sim_id, float* positions, float* velocities, int to_device,
                  double* a, int* steps_done, void* stream);
-/* 1 while the simulation still has steps to run, 0 when done, <0 if unknown id. */
+/* src/density.py:7-48 on a resident simulation: the CIC density of its current state into
+   rho (device, N_CELLS^3, [z][y][x]), the grid src/save_data.py:17-18 writes when
+   SAVE_DENSITY is set.  Deterministic (the deposit of pm_batch_step's step, written out). */
+int pm_batch_density(pm_batch* b, int sim_id, float* rho, void* stream);
+/* 1 while the simulation still has steps to run or its last steps are still running on the
+   device, 0 once its final state is complete, <0 if unknown id. */
 int pm_batch_active(pm_batch* b, int sim_id);
 int pm_batch_remove(pm_batch* b, int sim_id);
 int pm_batch_set_graphs(pm_batch* b, int enable);
@@ -192,6 +208,9 @@ int pm_batch_check(pm_batch* b, void* stream, int* bits);
 int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void* stream);
 /* Kernel launches per step for the resident simulations (-1 on error). */
 int pm_batch_launches_per_step(pm_batch* b);
+/* Host seconds the batch has spent so far (out[0..n-1], n <= 4): admissions, planning, CUDA
+   graph capture and instantiation, retirements. */
+int pm_batch_host_seconds(pm_batch* b, double* out, int n);
 
 #ifdef __cplusplus
 }

@@ -13,6 +13,8 @@ for p in (ROOT, PKG):
         sys.path.insert(0, p)
 
 GOLDEN_CASES = ["n8_g16", "n12_g24", "n16_g32", "n24_g48", "n32_g64"]
+# the 64^3-particle / 128^3-grid configuration: inputs whole, outputs sampled (make_golden.py)
+COMPACT_CASES = ["n64_g128"]
 
 
 def pytest_configure(config):

@@ -24,7 +24,8 @@ import types
 
 import numpy as np
 
-REF_SRC = os.environ.get("PM_REFERENCE_SRC", "/root/reference/src")
+# the reference's src/ directory (required: e.g. PM_REFERENCE_SRC=<checkout>/src)
+REF_SRC = os.environ.get("PM_REFERENCE_SRC")
 REF_MODULES = ["configure_me", "cosmology", "density", "fourier_utils", "potential",
                "integrate", "gaussian_random_field", "zeldovich"]
 
@@ -82,6 +83,8 @@ def load(overrides: dict):
 
     Returns a namespace object with the imported modules as attributes.
     """
+    if not REF_SRC or not os.path.isdir(REF_SRC):
+        raise RuntimeError("set PM_REFERENCE_SRC to the reference's src/ directory")
     for name in REF_MODULES + ["numba", "pyfftw"]:
         sys.modules.pop(name, None)
     tmp = tempfile.mkdtemp(prefix="pmref_")

@@ -51,12 +51,13 @@ def test_reference_arm_prints_from_rank_zero_only(capsys):
 
 
 def test_reference_arm_line_contract(capsys):
-    """Rank 0 of the reference arm prints one JSON line carrying the contract keys; its e2e
-    moves no host<->device bytes and its value is the CPU port's."""
+    """Rank 0 of the reference arm prints one JSON line carrying the contract keys; it times
+    the steps and warm-up asked for, its config has the GPU arm's keys, its e2e moves no
+    host<->device bytes and its value is the CPU port's."""
     import argparse
     import json
     import bench
-    args = argparse.Namespace(steps=2, cpu_steps=1, warmup=0, n_parts=8, n_cells=16, box=100.0)
+    args = argparse.Namespace(steps=2, cpu_steps=1, warmup=1, n_parts=8, n_cells=16, box=100.0)
     bench.run_reference(args, 1, 0)
     lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.strip()]
     assert len(lines) == 1
@@ -64,7 +65,9 @@ def test_reference_arm_line_contract(capsys):
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
                 "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert key in d, key
-    assert d["impl"] == "reference" and d["steps"] == 1 and d["value"] > 0
+    assert d["impl"] == "reference" and d["steps"] == 2 and d["warmup"] == 1 and d["value"] > 0
+    cfg = bench.workload_config(3, 8, 16, 100.0)
+    assert set(d["config"]) == set(bench.bench_config(cfg, 1, 0.0))
     assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT and d["higher_is_better"] is True
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert (d["config"]["n_parts"], d["config"]["n_cells"], d["config"]["box_size"]) == (8, 16, 100.0)

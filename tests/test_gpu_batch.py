@@ -108,6 +108,7 @@ def test_retire_and_admission(cuda):
     with pytest.raises(PMError):
         b.add(small_cfg(16, 3), *ics.initial_conditions(small_cfg(16, 3)))
     b.step(100)
+    cuda.cuda.synchronize()  # active() reports a simulation done once its last steps have run
     assert not b.active(s1) and not b.active(s2)
     assert b.state(s1)[1] == O.step_count(c1.a_init, c1.a_end, c1.steps)
     assert b.state(s2)[1] == O.step_count(c2.a_init, c2.a_end, c2.steps)

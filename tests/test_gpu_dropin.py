@@ -113,3 +113,32 @@ def test_pmesh_resident_writes_snapshots_in_the_background(cuda, restore_modules
     assert set(last) >= {"x1", "x2", "x3", "vx1", "vx2", "vx3", "a"}
     assert last["x1"].dtype == np.float32 and last["x1"].shape == (c["N_PARTS"] ** 3,)
     assert np.isfinite(last["vx3"]).all() and 0 < float(last["a"]) <= c["A_END"]
+
+
+def test_pmesh_snapshots_carry_the_density_in_both_modes(cuda, restore_modules, tmp_path, monkeypatch):
+    """SAVE_DENSITY: the resident engine writes the `density` dataset (save_data.py:17-18), the
+    density the last step before the snapshot was computed from (pmesh.py:60-67), as the loop
+    over the drop-in modules does."""
+    from pmgpu.snapshot import read_file
+    f, c = load_golden("n16_g32")
+    c = dict(c, STEPS=20)
+    out = {}
+    for resident in (False, True):
+        d = tmp_path / ("resident" if resident else "loop")
+        d.mkdir()
+        monkeypatch.chdir(d)
+        install_config(c, RESIDENT=resident, SAVE_DATA=True, SAVE_DENSITY=True, N_SAVE_FILES=4)
+        pmesh = importlib.import_module("pmesh")
+        pmesh.simulator()
+        for m in DROPIN:
+            sys.modules.pop(m, None)
+        out[resident] = {p.name: read_file(str(p)) for p in sorted((d / "Data").iterdir())}
+    assert sorted(out[True]) == sorted(out[False]) and len(out[True]) >= 4
+    mass = (c["N_CELLS"] / c["N_PARTS"]) ** 3 * c["N_PARTS"] ** 3
+    for name, snap in out[True].items():
+        if name.startswith("data.0."):  # the initial-conditions file holds the random field
+            continue
+        rho = snap["density"]
+        assert rho.shape == (c["N_CELLS"],) * 3
+        assert float(rho.sum(dtype=np.float64)) == pytest.approx(mass, rel=1e-6)
+        assert rel_l2(rho, out[False][name]["density"]) < 1e-4, name

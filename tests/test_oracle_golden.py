@@ -3,7 +3,7 @@ running the reference source, see tests/golden/make_golden.py).  CPU only."""
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, load_golden, periodic_maxdiff, rel_l2
+from conftest import COMPACT_CASES, GOLDEN_CASES, load_golden, periodic_maxdiff, rel_l2
 from oracle import pm_oracle as O
 
 
@@ -111,3 +111,28 @@ def test_cell_keys_order_rows_by_tile():
     rows = keys >> xb
     assert np.array_equal(rows, O.row_index(cells[1], cells[2], n))
     assert rows.max() < n * n
+
+
+@pytest.mark.parametrize("name", COMPACT_CASES)
+def test_oracle_matches_reference_64p_128g(name):
+    """The 64^3-particle / 128^3-grid configuration (box 100 Mpc/h, seed 0, 100 STEPS): one
+    step of the oracle against the reference's own outputs, at the fixture's sampled cells and
+    particles and through whole-grid sums."""
+    f, c = load_golden(name)
+    n = c["N_CELLS"]
+    mass = (n / c["N_PARTS"]) ** 3
+    idx, pidx = f["cell_idx"], f["part_idx"]
+    rho = O.density(f["pos0"], mass, n)
+    assert rel_l2(rho.reshape(-1)[idx], f["rho0_s"]) < 1e-6
+    assert rel_l2(rho.sum(axis=0), f["rho0_proj"]) < 1e-6
+    assert abs(rho.sum() - f["rho0_sum"]) < 1e-6 * f["rho0_sum"]
+    fg = O.fourier_grid(n)
+    phi = O.potential(rho, fg, f["a"][0], c["OMEGA_M0"])
+    assert rel_l2(phi.reshape(-1)[idx], f["phi0_s"]) < 1e-6
+    assert rel_l2(phi.sum(axis=0), f["phi0_proj"]) < 1e-6
+    da = (c["A_END"] - c["A_INIT"]) / c["STEPS"]
+    x, v = O.advance_time(rho, f["pos0"], f["vel0"], fg, f["a"][0], da, c["OMEGA_M0"], c["OMEGA_LAMBDA0"],
+                          c["OMEGA_K0"], c["H0"])
+    assert periodic_maxdiff(x[:, pidx], f["pos1_s"], n) < 4 * np.spacing(np.float32(n))
+    assert rel_l2(v[:, pidx], f["vel1_s"]) < 1e-6
+    assert rel_l2((v.astype(np.float64) ** 2).sum(axis=1), f["vel1_sq"]) < 1e-6
