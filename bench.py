@@ -168,6 +168,16 @@ def algorithmic_bytes(np_, n):
     }
 
 
+def bench_config(cfg, ws, t_ics):
+    """The `config` object of both arms' lines (same keys, same workload description)."""
+    return {"workload": WORKLOAD if (cfg.n_parts, cfg.n_cells) == (256, 512) else
+            f"reduced case: {cfg.n_parts}^3 particles, {cfg.n_cells}^3 grid",
+            "n_parts": cfg.n_parts, "n_cells": cfg.n_cells, "box_size": cfg.box_size, "a_init": cfg.a_init,
+            "da": cfg.da, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+            "l2": f"inputs larger than L2 ({cfg.n_cells}^3 grid = {4 * cfg.n_cells ** 3 / 1e6:.0f} MB per field)",
+            "ics_seconds": round(t_ics, 1)}
+
+
 def make_ics(cfg):
     from pmgpu import ics
     return ics.initial_conditions(cfg)
@@ -281,18 +291,19 @@ def run_gpu(args, ws, rank, local):
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(cfg, pos, vel, args.cpu_steps)
+    # the other two workloads of the metric, on the same GPU (single-GPU runs only)
+    batched = served = None
+    if ws == 1 and not args.plain_only:
+        batched = measure_batched(args, local)
+        served = measure_served(args, local, args.headline_serve_seconds)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": t_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic: seeded GRF + Zel'dovich ICs (reference algorithm)",
-        "config": {"workload": WORKLOAD if (cfg.n_parts, cfg.n_cells) == (256, 512) else
-                   f"reduced case: {cfg.n_parts}^3 particles, {cfg.n_cells}^3 grid",
-                   "n_parts": cfg.n_parts, "n_cells": cfg.n_cells, "box_size": cfg.box_size, "a_init": 0.02,
-                   "da": cfg.da, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (512^3 grid = 537 MB per field)", "ics_seconds": round(t_ics, 1)},
+        "config": bench_config(cfg, ws, t_ics),
         "e2e": e2e, "gpu_launches": launches * K, "roofline": roofline, "cpu_baseline": cpu,
-        "clocks": clk.summary(),
+        "clocks": clk.summary(), "batched": batched, "served": served,
     }
     print(json.dumps(line), flush=True)
     if dist is not None:
@@ -346,16 +357,29 @@ def batched_configs(count=64, seed=0):
     return out
 
 
-def run_batched(args, local):
-    """All simulations in one batch (one launch per phase, CUDA graphs) vs each one alone."""
+def batched_ics(cfgs, device):
+    """Initial conditions of every configuration, generated on the GPU (host draws only the
+    uniform pairs of the reference's rejection loop)."""
+    from pmgpu.device_ics import DeviceICs
+    gens, out = {}, []
+    for c in cfgs:
+        g = gens.get(c.n_parts) or gens.setdefault(c.n_parts, DeviceICs(c.n_parts, device))
+        out.append(g.generate(c))
+    for g in gens.values():
+        g.close()
+    return out
+
+
+def measure_batched(args, local):
+    """All simulations of the ensemble in one batch (one launch per phase, CUDA graphs)
+    against each one run alone, one after another: dict of the figures."""
     import torch
-    import pmgpu
     from pmgpu.batch import Batch
     from pmgpu.config import step_count
-    torch.cuda.set_device(local)
-    pmgpu.build()
     cfgs = batched_configs(args.batch_sims)
-    ics_ = _ics_pool(cfgs)
+    t0 = time.time()
+    ics_ = batched_ics(cfgs, local)
+    t_ics = time.time() - t0
     steps = [step_count(c.a_init, c.a_end, c.steps) for c in cfgs]
     pu = sum(c.np_total * k for c, k in zip(cfgs, steps))
     warm = Batch(device=local)
@@ -396,67 +420,81 @@ def run_batched(args, local):
             one.step(step_count(c.a_init, c.a_end, c.steps) + 1)
             one.close()
     t_plain = timed(plain)
-    line = {"metric": METRIC, "workload": "batched", "value": pu / t_batch, "unit": UNIT,
-            "plain_value": pu / t_plain, "batched_over_plain": t_plain / t_batch, "sims": len(cfgs),
-            "particle_updates": pu, "seconds_batched": round(t_batch, 3), "seconds_plain": round(t_plain, 3),
+    return {"value": pu / t_batch, "unit": UNIT, "plain_value": pu / t_plain,
+            "batched_over_plain": t_plain / t_batch, "sims": len(cfgs), "particle_updates": pu,
+            "seconds_batched": round(t_batch, 3), "seconds_plain": round(t_plain, 3), "ics_seconds": round(t_ics, 2),
             "batched_phase_ms": {k: round(v, 4) for k, v in prof.items()}, "launches_per_step": launches,
-            "dtype": "f32", "data": "synthetic: seeded GRF + Zel'dovich ICs (reference algorithm)",
-            "config": {"workload": f"{len(cfgs)} simulations, seeds 0-{len(cfgs) - 1}, N_PARTS in "
-                                   "{32,48,64,96,128}, grid 2N, box U(50,500) Mpc/h, 200 steps",
-                       "plain": "each simulation alone in its own resident batch, one after another"}}
+            "workload": f"{len(cfgs)} simulations, seeds 0-{len(cfgs) - 1}, N_PARTS in {{32,48,64,96,128}}, "
+                        "grid 2N, box U(50,500) Mpc/h, 200 steps, f32",
+            "plain": "each simulation alone in its own resident batch, one after another"}
+
+
+def measure_served(args, local, seconds):
+    """Poisson request stream against one GPU (continuous batching under a memory cap)."""
+    from pmgpu.serve import Server, poisson_stream, summarize
+    stream = poisson_stream(args.serve_rate, seconds, seed=0)
+    srv = Server(mem_cap_bytes=int(args.serve_cap_gb * 2 ** 30), ic_workers=args.ic_workers,
+                 steps_per_tick=args.steps_per_tick, device=local)
+    t0 = time.perf_counter()
+    res = srv.run(stream)
+    wall = time.perf_counter() - t0
+    host = srv.host_seconds()
+    srv.close()
+    summ = summarize(res, wall)
+    offered = sum(r.particle_updates for r in stream) / seconds
+    return {"value": summ["particle_updates_per_s"], "unit": UNIT, "p50_latency_s": summ["p50_latency_s"],
+            "p99_latency_s": summ["p99_latency_s"], "mean_latency_s": summ["mean_latency_s"],
+            "requests": summ["requests"], "offered_requests": len(stream),
+            "offered_particle_updates_per_s": offered, "wall_s": round(wall, 2), "host_seconds": host,
+            "workload": f"Poisson {args.serve_rate} req/s for {seconds} s, N_PARTS in {{64,96,128,192,256}} weighted "
+                        "40/25/20/10/5%, grid 2N, box U(100,500), steps U(50,500), f32",
+            "memory_cap_gb": args.serve_cap_gb, "steps_per_tick": args.steps_per_tick}
+
+
+def run_batched(args, local):
+    import pmgpu
+    import torch
+    torch.cuda.set_device(local)
+    pmgpu.build()
+    d = measure_batched(args, local)
+    line = {"metric": METRIC, "workload": "batched", **d, "dtype": "f32",
+            "data": "synthetic: seeded GRF + Zel'dovich ICs (reference algorithm)"}
     print(json.dumps(line), flush=True)
 
 
 def run_served(args, local):
-    """Poisson request stream against one GPU: continuous batching under a memory cap."""
-    import torch
     import pmgpu
-    from pmgpu.serve import Server, poisson_stream, summarize
+    import torch
     torch.cuda.set_device(local)
     pmgpu.build()
-    stream = poisson_stream(args.serve_rate, args.serve_seconds, seed=0)
-    srv = Server(mem_cap_bytes=int(args.serve_cap_gb * 2 ** 30), ic_workers=args.ic_workers,
-                 steps_per_tick=args.steps_per_tick, device=local)
-    t0 = time.perf_counter()
     with ClockSampler(local) as clk:
-        res = srv.run(stream)
-    wall = time.perf_counter() - t0
-    srv.close()
-    summ = summarize(res, wall)
-    offered = sum(r.particle_updates for r in stream) / args.serve_seconds
-    line = {"metric": METRIC, "workload": "served", "value": summ["particle_updates_per_s"], "unit": UNIT,
-            "p50_latency_s": summ["p50_latency_s"], "p99_latency_s": summ["p99_latency_s"],
-            "mean_latency_s": summ["mean_latency_s"], "requests": summ["requests"], "offered_requests": len(stream),
-            "offered_particle_updates_per_s": offered, "wall_s": round(wall, 2), "dtype": "f32",
-            "data": "synthetic request stream (seeded)",
-            "config": {"workload": f"Poisson {args.serve_rate} req/s for {args.serve_seconds} s, N_PARTS in "
-                                   "{64,96,128,192,256} weighted 40/25/20/10/5%, grid 2N, box U(100,500), "
-                                   "steps U(50,500)", "memory_cap_gb": args.serve_cap_gb,
-                       "steps_per_tick": args.steps_per_tick, "ic_workers": args.ic_workers},
+        d = measure_served(args, local, args.serve_seconds)
+    line = {"metric": METRIC, "workload": "served", **d, "dtype": "f32", "data": "synthetic request stream (seeded)",
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
 
 def run_reference(args, ws, rank):
+    """The reference's step on the host cores (its CPU port, see cpu_baseline): W untimed
+    full-size steps, then the K timed steps the command asks for, on the same workload and
+    with the same config keys as the GPU arm."""
     if rank != 0:
         return
-    import numpy as np  # noqa: F401
-    K = max(1, min(args.steps, args.cpu_steps))
-    cfg = workload_config(K, args.n_parts, args.n_cells, args.box)
+    K, W = max(1, args.steps), max(0, args.warmup)
+    cfg = workload_config(K + W, args.n_parts, args.n_cells, args.box)
+    t0 = time.time()
     pos, vel = make_ics(cfg)
-    if args.warmup > 0:
-        cpu_baseline(cfg, pos, vel, 1)
+    t_ics = time.time() - t0
+    if W > 0:
+        cpu_baseline(cfg, pos, vel, W)
     cb = cpu_baseline(cfg, pos, vel, K)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": ws, "steps": K,
-            "warmup": min(args.warmup, 1), "ms_per_step": cb["seconds"] * 1e3 / K, "higher_is_better": True,
+            "warmup": W, "ms_per_step": cb["seconds"] * 1e3 / K, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded GRF + Zel'dovich ICs (reference algorithm)",
-            "config": {"workload": WORKLOAD if (cfg.n_parts, cfg.n_cells) == (256, 512) else
-                       f"reduced case: {cfg.n_parts}^3 particles, {cfg.n_cells}^3 grid",
-                       "n_parts": cfg.n_parts, "n_cells": cfg.n_cells, "box_size": cfg.box_size,
-                       "note": "numba/pyFFTW are not installed: the reference step runs as its CPU port "
-                               "(C + OpenMP particle loops, scipy.fft, all host cores); steps bounded to a few "
-                               "full-size steps"},
+            "config": bench_config(cfg, ws, t_ics),
+            "note": "numba/pyFFTW are not installed: the reference step runs as its CPU port (C + OpenMP "
+                    "particle loops, scipy.fft complex128 FFTs, all host cores), full-size steps",
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -481,7 +519,12 @@ def main():
                          "request-stream workloads")
     ap.add_argument("--batch-sims", type=int, default=64)
     ap.add_argument("--serve-rate", type=float, default=20.0)
-    ap.add_argument("--serve-seconds", type=float, default=120.0)
+    ap.add_argument("--serve-seconds", type=float, default=120.0,
+                    help="arrival window of --workload served (the stream's specified 120 s)")
+    ap.add_argument("--headline-serve-seconds", type=float, default=20.0,
+                    help="arrival window of the served figures carried by the default (plain) line")
+    ap.add_argument("--plain-only", action="store_true",
+                    help="the plain line without its batched and served figures")
     ap.add_argument("--serve-cap-gb", type=float, default=150.0)
     ap.add_argument("--steps-per-tick", type=int, default=4)
     ap.add_argument("--ic-workers", type=int, default=12)
