@@ -48,6 +48,17 @@ struct SimRec {
 
 enum Phase { PH_KEYS = 0, PH_DEP, PH_KICK, PH_FIXED };
 
+// Schedule of the phases of one grid size, chosen by the autotuner (autotune below).  Every
+// choice leaves every result bit-identical: the deposit's integer sums do not depend on which
+// tiles run when or where, the fused and the separate deposit convert the same sums, and the
+// persistent kernels compute each work unit the same way whatever their grid.
+enum DepMode : int { DEP_FUSED_DENSE_FIRST = 0, DEP_FUSED_INDEX = 1, DEP_SEPARATE = 2 };
+struct Shape {
+  int dep = DEP_FUSED_DENSE_FIRST;  // deposit of the sizes that can fuse it with the x R2C
+  int dep_cps = 0;                  // fused deposit CTAs per SM (0: as many as fit)
+  int x_cps = 8;                    // CTAs per SM of the x passes' row transforms
+};
+
 struct Plan {
   int nsims = 0;
   long long ptot = 0;
@@ -58,12 +69,26 @@ struct Plan {
   std::vector<int> x_total, line_total;  // per distinct size
   std::vector<int> single;               // per distinct size: the only simulation of that size, or -1
   std::vector<int> fused, fdep_total;    // per distinct size: deposit fused with the x R2C, its tiles
+  std::vector<Shape> shape;              // per distinct size: the tuned schedule
+  int kick_cps = 16;                     // kick CTAs per SM
   int max_dep_smem = 0;
   int max_n = 0;
   long long sort_n = 0;  // slots the next step's sort reads (> ptot right after a retirement)
 };
 
 const int kStateArrays = 11;  // x y z vx vy vz id, cell record: cell fx fy fz
+
+// Schedules found by the autotuner, for the whole process: per (grid size, log2 of the size's
+// deposit tiles in the batch), and the kick's per log2 of its work units.
+std::mutex g_tune_lock;
+std::map<std::pair<int, int>, Shape> g_shapes;
+std::map<int, int> g_kick_cps;
+
+int ilog2(long long v) {
+  int b = 0;
+  while (v > 1) { v >>= 1; ++b; }
+  return b;
+}
 
 }  // namespace
 
@@ -88,6 +113,8 @@ struct pm_batch {
   Plan plan;
   bool dirty = true, keys_valid = false;
   bool graphs = true;
+  bool autotune = true;     // tune the schedule of new plans (see autotune)
+  bool tuned = false;       // the current plan's schedule is settled
   bool sparse = false;      // the state the next step reads has empty slots (after a retirement)
   long long in_total = 0;   // slots of that state
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
@@ -399,6 +426,21 @@ int build_plan(pm_batch* b, cudaStream_t st) {
             "prepare fused deposit");
   }
   PB_CK(deposit_prepare(), "prepare deposit");
+  {  // the schedule: tuned values from the process-wide cache, defaults for the rest
+    std::lock_guard<std::mutex> g(g_tune_lock);
+    b->tuned = true;
+    P.shape.assign(P.sizes.size(), Shape());
+    for (size_t i = 0; i < P.sizes.size(); ++i) {
+      const auto key = std::make_pair(P.sizes[i], ilog2(std::max(1, P.fdep_total[i] ? P.fdep_total[i] : P.x_total[i])));
+      auto it = g_shapes.find(key);
+      if (it != g_shapes.end()) P.shape[i] = it->second;
+      else b->tuned = false;
+      if (!P.fused[i]) P.shape[i].dep = DEP_SEPARATE;
+    }
+    auto kt = g_kick_cps.find(ilog2(std::max(1, P.fixed_total[PH_KICK])));
+    if (kt != g_kick_cps.end()) P.kick_cps = kt->second;
+    else b->tuned = false;
+  }
   drop_graphs(b);
   b->dirty = false;
   return PM_OK;
@@ -415,6 +457,32 @@ Work work_of(pm_batch* b, int ph, int total) {
 // Phases timed by pm_batch_profile, in launch order.
 enum ProfPhase { PP_SORT = 0, PP_ROWS, PP_DEPOSIT, PP_X_R2C, PP_Y_FWD, PP_Z_GREEN, PP_Y_INV, PP_X_C2R, PP_KICK,
                  PP_COEF, PP_COUNT };
+
+// The deposit of the simulations of distinct size g that can fuse it with the x R2C, on the
+// schedule `sh` (a separate deposit leaves the x R2C to the spectral phase).
+int enqueue_deposit(pm_batch* b, int g, const Shape& sh, Parts in, const unsigned* perm, cudaStream_t st) {
+  const Plan& P = b->plan;
+  const Sim* ds = b->d_sims.as<Sim>();
+  int* err = b->d_err.as<int>();
+  const int n = P.sizes[g], tot = P.fdep_total[g];
+  const Work wg = work_of(b, PH_FIXED + 3 * g + 2, tot);
+  if (sh.dep == DEP_SEPARATE) {
+    PB_CK(launch_deposit(ds, wg, in, perm, b->row_start.as<unsigned>(), POS_DISP, err, grid_for(tot, b->sms, 3),
+                         deposit_smem_bytes(n, TILE_Y, TILE_Z), st),
+          "deposit");
+    return PM_OK;
+  }
+  if (sh.dep == DEP_FUSED_DENSE_FIRST)
+    PB_CK(launch_tile_order(ds, wg, b->row_start.as<unsigned>(), b->tile_order.as<unsigned>(),
+                            b->tile_next.as<unsigned>() + 2, b->sms, st),
+          "tile order");
+  PB_CK(deposit_r2c_dispatch(n, ds, wg, in, perm, b->row_start.as<unsigned>(), POS_DISP, err,
+                             b->tile_next.as<unsigned>(),
+                             sh.dep == DEP_FUSED_DENSE_FIRST ? b->tile_order.as<unsigned>() : nullptr,
+                             grid_for(tot, b->sms, sh.dep_cps ? sh.dep_cps : deposit_r2c_ctas_per_sm(n)), st),
+        "fused deposit");
+  return PM_OK;
+}
 
 // Enqueue one step (state in b->st[cur] -> b->st[1 - cur]).  With `ev` (PP_COUNT + 1
 // events) an event is recorded before the first phase and after every phase.
@@ -438,28 +506,20 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
     PB_CK(launch_deposit(ds, work_of(b, PH_DEP, P.fixed_total[PH_DEP]), in, perm, b->row_start.as<unsigned>(),
                          POS_DISP, err, grid_for(P.fixed_total[PH_DEP], b->sms, 3), P.max_dep_smem, st),
           "deposit");
-  for (size_t g = 0; g < P.sizes.size(); ++g) {
-    if (!P.fused[g]) continue;
-    const int tot = P.fdep_total[g];
-    const Work wg = work_of(b, PH_FIXED + 3 * (int)g + 2, tot);
-    PB_CK(launch_tile_order(ds, wg, b->row_start.as<unsigned>(), b->tile_order.as<unsigned>(),
-                            b->tile_next.as<unsigned>() + 2, b->sms, st),
-          "tile order");
-    PB_CK(deposit_r2c_dispatch(P.sizes[g], ds, wg, in, perm, b->row_start.as<unsigned>(), POS_DISP, err,
-                               b->tile_next.as<unsigned>(), b->tile_order.as<unsigned>(),
-                               grid_for(tot, b->sms, deposit_r2c_ctas_per_sm(P.sizes[g])), st),
-          "fused deposit");
-  }
+  for (size_t g = 0; g < P.sizes.size(); ++g)
+    if (P.fused[g])
+      if (int r = enqueue_deposit(b, (int)g, P.shape[g], in, perm, st)) return r;
   PB_CK(mark(1 + PP_DEPOSIT), "event");
   const SpecKind order[5] = {SPEC_X_R2C, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Y_INV, SPEC_X_C2R};
   for (int o = 0; o < 5; ++o) {
     const SpecKind k = order[o];
     for (size_t g = 0; g < P.sizes.size(); ++g) {
-      if (k == SPEC_X_R2C && P.fused[g]) continue;
+      if (k == SPEC_X_R2C && P.shape[g].dep != DEP_SEPARATE) continue;  // done by the fused deposit
       const bool xk = (k == SPEC_X_R2C || k == SPEC_X_C2R);
       const int ph = PH_FIXED + 3 * (int)g + (xk ? 0 : 1);
       const int tot = xk ? P.x_total[g] : P.line_total[g];
-      PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot), grid_for(tot, b->sms, 8), st,
+      PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot),
+                              xk ? grid_for(tot, b->sms, P.shape[g].x_cps) : grid_for(tot, b->sms, 8), st,
                               b->d_maps.as<CUtensorMap>(), err),
             "spectral");
     }
@@ -468,7 +528,8 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
   // the kick writes the next keys and counts them per row for the next step's sort
   PB_CK(cudaMemsetAsync(b->row_count.p, 0, sizeof(unsigned) * (size_t)P.rows, st), "count reset");
   PB_CK(launch_kick(ds, work_of(b, PH_KICK, P.fixed_total[PH_KICK]), in, out, perm, b->sort.keys.as<unsigned>(),
-                    POS_DISP, err, grid_for(P.fixed_total[PH_KICK], b->sms, 16), st, b->row_count.as<unsigned>()),
+                    POS_DISP, err, grid_for(P.fixed_total[PH_KICK], b->sms, P.kick_cps), st,
+                    b->row_count.as<unsigned>()),
         "kick");
   PB_CK(mark(1 + PP_KICK), "event");
   PB_CK(launch_coef(b->d_sims.as<Sim>(), P.nsims, 1, st), "coef");
@@ -482,8 +543,10 @@ int launches_per_step(pm_batch* b) {
   // counting sort: 3 scan kernels and the scatter (the kick makes the histogram; the count
   // reset is a memset)
   int n = 4 + (P.fixed_total[PH_DEP] > 0 ? 1 : 0) + 5 * (int)P.sizes.size() + 1 + 1;
-  // each fused size replaces its x R2C launch by the fused deposit, preceded by its tile order
-  for (int f : P.fused) n += f;
+  // a fused size replaces its x R2C launch by the fused deposit (with a dense-first tile
+  // order, one launch more); a separate one adds its deposit launch
+  for (size_t g = 0; g < P.sizes.size(); ++g)
+    if (P.fused[g]) n += P.shape[g].dep == DEP_FUSED_INDEX ? 0 : 1;
   return n;
 }
 
@@ -500,6 +563,127 @@ int ensure_keys(pm_batch* b, cudaStream_t st) {
                       b->sms, st),
         "row histogram");
   b->keys_valid = true;
+  return PM_OK;
+}
+
+// Autotuner: for each grid size of the plan whose schedule is not in the process-wide cache,
+// and for the kick, time the candidate schedules on the batch's own data (one warm-up launch,
+// then the mean of three) and keep the fastest.  The candidates are the deposit modes (fused
+// with dense-first tiles, fused in index order, separate from the x R2C), the fused deposit's
+// CTAs per SM, the x passes' CTAs per SM and the kick's.  Runs between steps: the trials write
+// only buffers that the next step rewrites from scratch (spectra, grids, the next state, tile
+// counters) or scratch (the kick's keys and histogram go to unused sort buffers), never the
+// state the step reads or the histogram its sort consumes.
+int autotune(pm_batch* b, cudaStream_t st) {
+  Plan& P = b->plan;
+  if (b->tuned || !b->autotune) return PM_OK;
+  HostTimer timer(b->host_s[1]);
+  const Sim* ds = b->d_sims.as<Sim>();
+  int* err = b->d_err.as<int>();
+  Parts in = state(b, b->cur), out = state(b, 1 - b->cur);
+  unsigned* perm = b->sort.vals.as<unsigned>();
+  // the row starts and permutation of the current keys (the step recomputes the same)
+  PB_CK(row_counting_sort(b->sort.keys.as<unsigned>(), P.sort_n, P.rows, b->row_count.as<unsigned>(),
+                          b->row_start.as<unsigned>(), b->row_cursor.as<unsigned>(), b->scan_sums.as<unsigned>(),
+                          perm, err, b->sms, st, nullptr, true),
+        "sort");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  PB_CK(cudaEventCreate(&e0), "event");
+  PB_CK(cudaEventCreate(&e1), "event");
+  int rc = PM_OK;
+  // mean milliseconds of `launch` (a callable returning a PM status)
+  auto time3 = [&](auto&& launch, float& ms) -> int {
+    if (int r = launch()) return r;
+    PB_CK(cudaEventRecord(e0, st), "event");
+    for (int i = 0; i < 3; ++i)
+      if (int r = launch()) return r;
+    PB_CK(cudaEventRecord(e1, st), "event");
+    PB_CK(cudaEventSynchronize(e1), "tune sync");
+    PB_CK(cudaEventElapsedTime(&ms, e0, e1), "event");
+    ms /= 3.f;
+    return PM_OK;
+  };
+  std::vector<std::pair<std::pair<int, int>, Shape>> found;
+  for (size_t g = 0; g < P.sizes.size() && !rc; ++g) {
+    const int n = P.sizes[g];
+    const auto key = std::make_pair(n, ilog2(std::max(1, P.fdep_total[g] ? P.fdep_total[g] : P.x_total[g])));
+    {
+      std::lock_guard<std::mutex> lk(g_tune_lock);
+      if (g_shapes.count(key)) continue;
+    }
+    Shape best = P.shape[g];
+    const Work wx = work_of(b, PH_FIXED + 3 * (int)g, P.x_total[g]);
+    if (P.fused[g]) {  // deposit mode and grid (a separate deposit is timed with its x R2C)
+      const int occ = deposit_r2c_ctas_per_sm(n);
+      std::vector<Shape> cands;
+      for (int cps = occ; cps >= 1; --cps) cands.push_back(Shape{DEP_FUSED_DENSE_FIRST, cps, best.x_cps});
+      cands.push_back(Shape{DEP_FUSED_INDEX, occ, best.x_cps});
+      cands.push_back(Shape{DEP_SEPARATE, occ, best.x_cps});
+      float best_ms = 1e30f;
+      for (const Shape& c : cands) {
+        float ms = 0.f;
+        rc = time3([&]() -> int {
+          if (int r = enqueue_deposit(b, (int)g, c, in, perm, st)) return r;
+          if (c.dep == DEP_SEPARATE)
+            PB_CK(spectral_dispatch(SPEC_X_R2C, n, ds, wx, grid_for(wx.total, b->sms, c.x_cps), st,
+                                    b->d_maps.as<CUtensorMap>(), err),
+                  "x r2c");
+          return PM_OK;
+        }, ms);
+        if (rc) break;
+        if (ms < best_ms) { best_ms = ms; best.dep = c.dep; best.dep_cps = c.dep_cps; }
+      }
+    }
+    if (!rc && xrow_supported(n)) {  // x passes' grid (register row transforms)
+      float best_ms = 1e30f;
+      for (int cps : {4, 8, 16}) {
+        float ms = 0.f;
+        rc = time3([&]() -> int {
+          PB_CK(spectral_dispatch(SPEC_X_C2R, n, ds, wx, grid_for(wx.total, b->sms, cps), st,
+                                  b->d_maps.as<CUtensorMap>(), err),
+                "x c2r");
+          return PM_OK;
+        }, ms);
+        if (rc) break;
+        if (ms < best_ms) { best_ms = ms; best.x_cps = cps; }
+      }
+    }
+    if (!rc) {
+      P.shape[g] = best;
+      found.emplace_back(key, best);
+    }
+  }
+  const int kkey = ilog2(std::max(1, P.fixed_total[PH_KICK]));
+  bool kick_known;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_lock);
+    kick_known = g_kick_cps.count(kkey) != 0;
+  }
+  if (!rc && !kick_known) {  // the kick's grid; its keys and histogram go to scratch buffers
+    const Work wk = work_of(b, PH_KICK, P.fixed_total[PH_KICK]);
+    float best_ms = 1e30f;
+    for (int cps : {4, 8, 16, 32}) {
+      float ms = 0.f;
+      rc = time3([&]() -> int {
+        PB_CK(launch_kick(ds, wk, in, out, perm, b->sort.vals_alt.as<unsigned>(), POS_DISP, err,
+                          grid_for(wk.total, b->sms, cps), st, b->row_cursor.as<unsigned>()),
+              "kick");
+        return PM_OK;
+      }, ms);
+      if (rc) break;
+      if (ms < best_ms) { best_ms = ms; P.kick_cps = cps; }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_lock);
+    for (auto& f : found) g_shapes[f.first] = f.second;
+    if (!kick_known) g_kick_cps[kkey] = P.kick_cps;
+  }
+  b->tuned = true;
+  drop_graphs(b);
   return PM_OK;
 }
 
@@ -783,6 +967,7 @@ int pm_batch_step(pm_batch* b, int nsteps, void* stream) {
     for (auto& s : b->sims) k = std::min(k, s->nsteps - s->done);
     if (k <= 0) break;
     if (int r = ensure_keys(b, st)) return r;
+    if (int r = autotune(b, st)) return r;
     if (int r = run_steps(b, k, st)) return r;
     for (auto& s : b->sims) {
       for (int i = 0; i < k; ++i) s->a += s->da;
@@ -922,6 +1107,33 @@ int pm_batch_remove(pm_batch* b, int sim_id) {
   return bfail(b, PM_ERR_ARG, "unknown simulation id");
 }
 
+int pm_batch_set_autotune(pm_batch* b, int enable) {
+  if (!b) return PM_ERR_ARG;
+  b->autotune = enable != 0;
+  if (!b->autotune) b->dirty = true;  // back to the defaults and cached schedules at the next plan
+  return PM_OK;
+}
+
+int pm_batch_schedule(pm_batch* b, int* out, int cap) {
+  if (!b || !out || cap < 0) return -1;
+  const Plan& P = b->plan;
+  int k = 0;
+  for (size_t g = 0; g < P.sizes.size() && k + 4 <= cap; ++g) {
+    const Shape& sh = P.shape.size() > g ? P.shape[g] : Shape();
+    out[k++] = P.sizes[g];
+    out[k++] = sh.dep;
+    out[k++] = sh.dep_cps ? sh.dep_cps : deposit_r2c_ctas_per_sm(P.sizes[g]);
+    out[k++] = sh.x_cps;
+  }
+  if (k + 4 <= cap && !P.sizes.empty()) {
+    out[k++] = 0;
+    out[k++] = P.kick_cps;
+    out[k++] = b->tuned ? 1 : 0;
+    out[k++] = 0;
+  }
+  return k;
+}
+
 int pm_batch_host_seconds(pm_batch* b, double* out, int n) {
   if (!b || !out || n < 0) return PM_ERR_ARG;
   for (int i = 0; i < n && i < 4; ++i) out[i] = b->host_s[i];
@@ -941,6 +1153,7 @@ int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void*
   int k = nsteps;
   for (auto& s : b->sims) k = std::min(k, s->nsteps - s->done);
   if (int r = ensure_keys(b, st)) return r;
+  if (int r = autotune(b, st)) return r;
   cudaEvent_t ev[PP_COUNT + 1];
   for (auto& e : ev) PB_CK(cudaEventCreate(&e), "event");
   int rc = PM_OK;

@@ -167,6 +167,7 @@ cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned*
                                int mode, int* err, unsigned* next_tile, const unsigned* order, int ctas,
                                cudaStream_t st);
 bool deposit_r2c_supported(int n);
+bool xrow_supported(int n);  // the x passes of size n transform rows in registers (their grid is tunable)
 int deposit_r2c_ctas_per_sm(int n);  // resident CTAs per SM of the fused deposit
 cudaError_t deposit_r2c_dispatch(int n, const Sim* sims, Work w, Parts p, const unsigned* perm,
                                  const unsigned* row_start, int mode, int* err, unsigned* next_tile,

@@ -944,7 +944,8 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
   const int grid = w.total < device_sms() ? w.total : device_sms();
   if constexpr (xrow_ok(N)) {
     if (kind == SPEC_X_R2C || kind == SPEC_X_C2R) {
-      const int per = xrow_nt(N) / 32, want = (w.total + per - 1) / per, cap = device_sms() * 8;
+      // ctas: the cap on the CTAs of the persistent row transform (the batch engine tunes it)
+      const int per = xrow_nt(N) / 32, want = (w.total + per - 1) / per, cap = ctas > 0 ? ctas : device_sms() * 8;
       const int g = want < cap ? want : cap;
       if (kind == SPEC_X_R2C) k_x_row<N, false><<<g, xrow_nt(N), 0, st>>>(sims, w);
       else k_x_row<N, true><<<g, xrow_nt(N), 0, st>>>(sims, w);

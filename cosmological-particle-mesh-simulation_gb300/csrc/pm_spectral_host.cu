@@ -33,6 +33,7 @@ bool spectral_encode_maps(int n, const void* spec, CUtensorMap out[2]) {
 }
 
 bool deposit_r2c_supported(int n) { return spectral_supported(n) && deposit_r2c_ok(n); }
+bool xrow_supported(int n) { return spectral_supported(n) && xrow_ok(n); }
 
 int deposit_r2c_ctas_per_sm(int n) { return xrow_ok(n) ? 3 : 2; }
 

@@ -74,6 +74,8 @@ SIGNATURES = {
     "pm_batch_profile": (c_int, [c_void_p, c_int, ctypes.POINTER(ctypes.c_float), c_int, c_void_p]),
     "pm_batch_launches_per_step": (c_int, [c_void_p]),
     "pm_batch_host_seconds": (c_int, [c_void_p, P_double, c_int]),
+    "pm_batch_set_autotune": (c_int, [c_void_p, c_int]),
+    "pm_batch_schedule": (c_int, [c_void_p, P_int, c_int]),
 }
 PROFILE_PHASES = ("sort", "rows", "deposit", "x_r2c", "y_fwd", "z_green", "y_inv", "x_c2r", "kick", "coef")
 

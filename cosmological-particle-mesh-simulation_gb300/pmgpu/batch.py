@@ -14,7 +14,7 @@ class Batch:
     """Wraps pm_batch_*.  Simulations are admitted from absolute (3, N_PARTS^3) float32
     positions / velocities (numpy on the host or CUDA tensors) and advance together."""
 
-    def __init__(self, device: int = 0, mem_cap_bytes: int = 0, graphs: bool = True):
+    def __init__(self, device: int = 0, mem_cap_bytes: int = 0, graphs: bool = True, autotune: bool = True):
         self._lib = _lib.load()
         self.device = device
         torch.cuda.init()
@@ -27,6 +27,8 @@ class Batch:
         self.cfgs: dict[int, Config] = {}
         if not graphs:
             self._lib.pm_batch_set_graphs(self._h, 0)
+        if not autotune:
+            self._lib.pm_batch_set_autotune(self._h, 0)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -129,6 +131,25 @@ class Batch:
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         self._check(self._lib.pm_batch_profile(self._h, int(nsteps), arr, len(arr), stream))
         return dict(zip(_lib.PROFILE_PHASES, [float(x) for x in arr]))
+
+    def set_autotune(self, enable: bool):
+        self._check(self._lib.pm_batch_set_autotune(self._h, 1 if enable else 0))
+
+    def schedule(self) -> list:
+        """The current plan's launch schedule per grid size (tuned or default) and the kick's."""
+        arr = (ctypes.c_int * 256)()
+        k = self._lib.pm_batch_schedule(self._h, arr, 256)
+        if k < 0:
+            raise _lib.PMError(k, "pm_batch_schedule failed")
+        modes = {0: "fused, dense tiles first", 1: "fused, index order", 2: "separate deposit + x R2C"}
+        out = []
+        for i in range(0, k, 4):
+            n, a, c, d = arr[i:i + 4]
+            if n == 0:
+                out.append({"kick_ctas_per_sm": a, "tuned": bool(c)})
+            else:
+                out.append({"n_cells": n, "deposit": modes.get(a, a), "deposit_ctas_per_sm": c, "x_ctas_per_sm": d})
+        return out
 
     def host_seconds(self) -> dict:
         """Host time spent so far in admissions, planning, graph capture and retirements."""

@@ -208,6 +208,17 @@ int pm_batch_check(pm_batch* b, void* stream, int* bits);
 int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void* stream);
 /* Kernel launches per step for the resident simulations (-1 on error). */
 int pm_batch_launches_per_step(pm_batch* b);
+/* The launch schedule of each grid size is tuned on the batch's own data when a plan meets a
+   size (and work volume) it has not timed before in this process: deposit fused with the x
+   R2C (dense tiles first or in index order) or separate, CTAs per SM of the fused deposit, of
+   the x passes and of the kick.  Every candidate gives bit-identical results.  enable = 0 keeps
+   the defaults (and schedules already tuned).  No counterpart in the reference: its FFTs are
+   planned by FFTW (src/potential.py:20,27). */
+int pm_batch_set_autotune(pm_batch* b, int enable);
+/* The current plan's schedule: 4 ints per grid size (n, deposit mode 0 fused dense-first /
+   1 fused index order / 2 separate, fused-deposit CTAs per SM, x-pass CTAs per SM), then
+   (0, kick CTAs per SM, 1 if tuned, 0).  Returns the ints written (-1 on error). */
+int pm_batch_schedule(pm_batch* b, int* out, int cap);
 /* Host seconds the batch has spent so far (out[0..n-1], n <= 4): admissions, planning, CUDA
    graph capture and instantiation, retirements. */
 int pm_batch_host_seconds(pm_batch* b, double* out, int n);

@@ -116,3 +116,67 @@ def test_retire_and_admission(cuda):
     b.remove(s2)
     s3 = b.add(small_cfg(16, 3), *ics.initial_conditions(small_cfg(16, 3)))
     assert b.active(s3)
+
+
+def test_autotuned_schedules_give_identical_results(cuda):
+    """The autotuner times its candidate schedules (deposit fused with dense tiles first or in
+    index order, or separate; CTAs per SM of the deposit, the x passes and the kick) on the
+    batch's own data between steps and keeps the fastest.  Every candidate, and the trials
+    themselves, leave the results bit-identical: a tuned batch and an untuned one end in the
+    same state."""
+    from pmgpu.batch import Batch
+    from pmgpu import ics
+    cfgs = [small_cfg(32, 11, box=150.0), small_cfg(16, 12), small_cfg(24, 13, box=90.0)]
+    ics_ = [ics.initial_conditions(c) for c in cfgs]
+    out = {}
+    for tune in (True, False):
+        b = Batch(autotune=tune)
+        ids = [b.add(c, p, v) for c, (p, v) in zip(cfgs, ics_)]
+        b.step(6)
+        b.check_device()
+        sched = b.schedule()
+        out[tune] = [b.get(i)[:2] for i in ids]
+        b.close()
+        sizes = sorted(e["n_cells"] for e in sched if "n_cells" in e)
+        assert sizes == [32, 48, 64]
+        kick = [e for e in sched if "kick_ctas_per_sm" in e]
+        assert len(kick) == 1 and kick[0]["kick_ctas_per_sm"] in (4, 8, 16, 32)
+        if tune:
+            assert kick[0]["tuned"]
+    for (p1, v1), (p2, v2) in zip(out[True], out[False]):
+        assert np.array_equal(p1, p2) and np.array_equal(v1, v2)
+
+
+def test_retired_simulation_leaves_without_disturbing_the_others(cuda):
+    """A simulation that finishes leaves the batch without a copy of the others' state: its
+    slots stay empty for one step (no keys, skipped by the sort) and the next kick writes the
+    survivors back compactly.  The survivors' states are those of a batch without it, and a
+    simulation admitted afterwards runs as it would alone."""
+    from pmgpu.batch import Batch
+    from pmgpu import ics
+    short, long_, late = small_cfg(16, 21, steps=5), small_cfg(24, 22, steps=40), small_cfg(16, 23, steps=40)
+    ic = {c.random_seed: ics.initial_conditions(c) for c in (short, long_, late)}
+    b = Batch()
+    s_short = b.add(short, *ic[21])
+    s_long = b.add(long_, *ic[22])
+    b.step(6)   # the short one runs its 4 steps and leaves
+    s_late = b.add(late, *ic[23])
+    b.step(9)
+    b.check_device()
+    cuda.cuda.synchronize()
+    assert not b.active(s_short) and b.active(s_long) and b.active(s_late)
+    got_long, got_late = b.get(s_long)[:2], b.get(s_late)[:2]
+    assert b.state(s_short)[1] == O.step_count(short.a_init, short.a_end, short.steps)
+    b.close()
+    alone = Batch()
+    a = alone.add(long_, *ic[22])
+    alone.step(15)
+    ref_long = alone.get(a)[:2]
+    alone.close()
+    alone = Batch()
+    a = alone.add(late, *ic[23])
+    alone.step(9)
+    ref_late = alone.get(a)[:2]
+    alone.close()
+    for got, ref in ((got_long, ref_long), (got_late, ref_late)):
+        assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
