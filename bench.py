@@ -211,7 +211,7 @@ def run_gpu(args, ws, rank, local):
 
     # ---- warm-up on a throwaway batch (W steps, graphs instantiated), then a per-phase
     # CUDA-event profile of the next steps of that run ----------------------------------
-    wb = Batch(device=local)
+    wb = Batch(device=local, autotune=not args.no_autotune)
     wb.add(cfg, pos, vel)
     wb.step(max(W, 1))
     prof = wb.profile(args.profile_steps)
@@ -220,7 +220,7 @@ def run_gpu(args, ws, rank, local):
     del wb
 
     # ---- timed: K steps of a fresh run from the ICs --------------------------------
-    b = Batch(device=local)
+    b = Batch(device=local, autotune=not args.no_autotune)
     sid = b.add(cfg, pos, vel)
     b.step(0)
     launches = b.launches_per_step()
@@ -387,13 +387,13 @@ def measure_batched(args, local):
     warm = Batch(device=local)
     for c, (p, v) in zip(cfgs, ics_):
         warm.add(c, p, v)
-    warm.step(2)
+    warm.step(4)  # (a plan is tuned once it has run two steps)
     schedule = warm.schedule()
     warm.close()
     for c, (p, v) in zip(cfgs, ics_):  # and each simulation alone, for the comparison run
         one = Batch(device=local)
         one.add(c, p, v)
-        one.step(1)
+        one.step(3)
         one.close()
     stream = torch.cuda.Stream()
 
@@ -483,6 +483,43 @@ def run_served(args, local):
     print(json.dumps(line), flush=True)
 
 
+def run_gradient(args, local):
+    """The force of the step two ways on the same state: the reference's central differences of
+    phi (32 taps per particle) and the spectral gradient (three force grids, 8 taps per axis),
+    each as pm_step on device arrays (K steps after W, CUDA events)."""
+    import dataclasses
+    import pmgpu
+    import torch
+    from pmgpu.context import PMContext
+    torch.cuda.set_device(local)
+    pmgpu.build()
+    cfg = workload_config(args.steps + args.warmup, args.n_parts, args.n_cells, args.box)
+    pos, vel = make_ics(cfg)
+    res = {}
+    for name, c in (("central_difference", cfg), ("spectral_gradient", dataclasses.replace(cfg, spectral_gradient=True))):
+        ctx = PMContext(c, device=local)
+        p, v = torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda()
+        a = cfg.a_init
+        for _ in range(args.warmup):
+            ctx.step(p, v, cfg.mass, a, cfg.da)
+            a += cfg.da
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            ctx.step(p, v, cfg.mass, a, cfg.da)
+            a += cfg.da
+        e1.record()
+        torch.cuda.synchronize()
+        ctx.check_device()
+        ms = e0.elapsed_time(e1) / args.steps
+        res[name] = {"ms_per_step": round(ms, 4), "value": cfg.np_total / (ms / 1e3)}
+        ctx.close()
+    line = {"metric": METRIC, "workload": "gradient", "unit": UNIT, "steps": args.steps, "warmup": args.warmup,
+            **res, "config": bench_config(cfg, 1, 0.0), "api": "pm_step on device arrays (drop-in step)"}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, ws, rank):
     """The reference's step on the host cores (its CPU port, see cpu_baseline): W untimed
     full-size steps, then the K timed steps the command asks for, on the same workload and
@@ -523,7 +560,7 @@ def main():
     ap.add_argument("--n-parts", type=int, default=256, help="reduced cases for profiling only")
     ap.add_argument("--n-cells", type=int, default=512)
     ap.add_argument("--box", type=float, default=250.0)
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served", "gradient"],
                     help="plain: the README workload (headline); batched / served: the ensemble and "
                          "request-stream workloads")
     ap.add_argument("--batch-sims", type=int, default=64)
@@ -532,6 +569,8 @@ def main():
                     help="arrival window of --workload served (the stream's specified 120 s)")
     ap.add_argument("--headline-serve-seconds", type=float, default=20.0,
                     help="arrival window of the served figures carried by the default (plain) line")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the batch engine's default launch schedule (fixed launch order, for profiling)")
     ap.add_argument("--plain-only", action="store_true",
                     help="the plain line without its batched and served figures")
     ap.add_argument("--serve-cap-gb", type=float, default=150.0)
@@ -547,6 +586,9 @@ def main():
     elif args.workload == "served":
         if rank == 0:
             run_served(args, local)
+    elif args.workload == "gradient":
+        if rank == 0:
+            run_gradient(args, local)
     else:
         run_gpu(args, ws, rank, local)
 

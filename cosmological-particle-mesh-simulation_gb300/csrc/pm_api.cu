@@ -18,6 +18,10 @@ struct pm_ctx {
   DBuf pk_partial, pk_out;            // power spectrum scratch
   DBuf row_count, row_cursor, scan_sums;  // counting sort of row keys
   DBuf spos, svel;                        // the state in row order (drop-in step)
+  // spectral gradient: spectra and force grids of the y and z axes (x uses spec and phi), the
+  // three descriptors of the inverse passes and their work tables and tensor maps
+  DBuf gspec[2], ggrid[2], d_sim3, d_prefix3, d_maps3;
+  const void* maps3_for = nullptr;
   cudaStream_t side = nullptr;            // velocity copy of pm_step_host
   cudaEvent_t ev_start = nullptr, ev_vel = nullptr;
   std::vector<double> pk_host;
@@ -63,6 +67,7 @@ Sim base_sim(pm_ctx* c, long long np) {
   s.part_off = 0;
   s.row_base = 0;
   s.s2 = c->tab.s2.as<float>();
+  s.sn = c->tab.sn.as<float>();
   s.tw = c->tab.tw.as<float2>();
   s.om = c->cfg.omega_m0;
   s.ol = c->cfg.omega_lambda0;
@@ -164,7 +169,9 @@ int deposit(pm_ctx* c, Call& k, unsigned* perm, cudaStream_t st) {
   return PM_OK;
 }
 
-int spectral(pm_ctx* c, Call& k, bool table, cudaStream_t st, bool skip_r2c = false) {
+int gradient_solve(pm_ctx* c, Call& k, cudaStream_t st);
+
+int spectral(pm_ctx* c, Call& k, bool table, cudaStream_t st, bool skip_r2c = false, bool gradient = false) {
   const Sim* ds = c->d_sim.as<Sim>();
   const int n = c->n;
   const int gx = grid_for(k.prefix[PH_X][1], c->sms, 8), gl = grid_for(k.prefix[PH_LINE][1], c->sms, 8);
@@ -172,10 +179,64 @@ int spectral(pm_ctx* c, Call& k, bool table, cudaStream_t st, bool skip_r2c = fa
   int* err = c->d_err.as<int>();
   if (!skip_r2c) PM_CK(spectral_dispatch(SPEC_X_R2C, n, ds, work(c, k, PH_X), gx, st, maps, err), "x r2c");
   PM_CK(spectral_dispatch(SPEC_Y_FWD, n, ds, work(c, k, PH_LINE), gl, st, maps, err), "y fwd");
+  if (gradient) return gradient_solve(c, k, st);
   PM_CK(spectral_dispatch(table ? SPEC_Z_TABLE : SPEC_Z_GREEN, n, ds, work(c, k, PH_LINE), gl, st, maps, err),
         "z green");
   PM_CK(spectral_dispatch(SPEC_Y_INV, n, ds, work(c, k, PH_LINE), gl, st, maps, err), "y inv");
   PM_CK(spectral_dispatch(SPEC_X_C2R, n, ds, work(c, k, PH_X), gx, st, maps, err), "x c2r");
+  return PM_OK;
+}
+
+// The spectral gradient (PM_FLAG_SPECTRAL_GRADIENT): from the spectrum after the forward y
+// pass, three copies go through the z pass with the Green function times -i sin(k_d) and the
+// inverse y and x passes -- one launch each over three descriptors -- into phi (x) and two more
+// grids (y, z); k.sim.grad then points the kick at them.
+int gradient_solve(pm_ctx* c, Call& k, cudaStream_t st) {
+  const int n = c->n;
+  const size_t sb = (size_t)n * n * spec_pitch(n) * sizeof(float2), gb = (size_t)n * n * n * sizeof(float);
+  for (int i = 0; i < 2; ++i) {
+    PM_CK(c->gspec[i].ensure(sb), "alloc gradient spectrum");
+    PM_CK(c->ggrid[i].ensure(gb), "alloc gradient grid");
+  }
+  PM_CK(c->d_sim3.ensure(3 * sizeof(Sim)), "alloc descriptors");
+  PM_CK(c->d_prefix3.ensure(8 * sizeof(int)), "alloc work");
+  const CUtensorMap* maps = nullptr;
+  if (c->maps_for && c->maps3_for != c->gspec[1].p) {  // tensor maps of the three spectra
+    CUtensorMap m[6];
+    const void* specs[3] = {c->spec.p, c->gspec[0].p, c->gspec[1].p};
+    bool ok = true;
+    for (int i = 0; i < 3; ++i) ok = ok && spectral_encode_maps(n, specs[i], &m[2 * i]);
+    c->maps3_for = nullptr;
+    if (ok) {
+      PM_CK(c->d_maps3.ensure(sizeof(m)), "alloc maps");
+      PM_CK(cudaMemcpy(c->d_maps3.p, m, sizeof(m), cudaMemcpyHostToDevice), "tensor maps");
+      c->maps3_for = c->gspec[1].p;
+    }
+  }
+  if (c->maps_for && c->maps3_for == c->gspec[1].p) maps = c->d_maps3.as<CUtensorMap>();
+  Sim s3[3];
+  for (int i = 0; i < 3; ++i) {
+    s3[i] = k.sim;
+    s3[i].grad_axis = i + 1;
+    s3[i].spec = i == 0 ? c->spec.as<float2>() : c->gspec[i - 1].as<float2>();
+    s3[i].phi = i == 0 ? c->phi.as<float>() : c->ggrid[i - 1].as<float>();
+  }
+  const int lu = (int)spectral_units(SPEC_Y_FWD, n), xu = (int)spectral_units(SPEC_X_C2R, n);
+  const int pre[8] = {0, lu, 2 * lu, 3 * lu, 0, xu, 2 * xu, 3 * xu};
+  PM_CK(cudaMemcpyAsync(c->d_sim3.p, s3, sizeof(s3), cudaMemcpyHostToDevice, st), "upload descriptors");
+  PM_CK(cudaMemcpyAsync(c->d_prefix3.p, pre, sizeof(pre), cudaMemcpyHostToDevice, st), "upload work");
+  PM_CK(cudaMemcpyAsync(c->gspec[0].p, c->spec.p, sb, cudaMemcpyDeviceToDevice, st), "copy spectrum");
+  PM_CK(cudaMemcpyAsync(c->gspec[1].p, c->spec.p, sb, cudaMemcpyDeviceToDevice, st), "copy spectrum");
+  const Sim* ds = c->d_sim3.as<Sim>();
+  const Work wl{c->d_prefix3.as<int>(), 3, 3 * lu}, wx{c->d_prefix3.as<int>() + 4, 3, 3 * xu};
+  const int gl = grid_for(wl.total, c->sms, 8), gx = grid_for(wx.total, c->sms, 8);
+  int* err = c->d_err.as<int>();
+  PM_CK(spectral_dispatch(SPEC_Z_GRAD, n, ds, wl, gl, st, maps, err), "z green gradient");
+  PM_CK(spectral_dispatch(SPEC_Y_INV, n, ds, wl, gl, st, maps, err), "y inv");
+  PM_CK(spectral_dispatch(SPEC_X_C2R, n, ds, wx, gx, st, maps, err), "x c2r");
+  k.sim.grad[0] = c->phi.as<float>();
+  k.sim.grad[1] = c->ggrid[0].as<float>();
+  k.sim.grad[2] = c->ggrid[1].as<float>();
   return PM_OK;
 }
 
@@ -278,6 +339,10 @@ void pm_ctx_destroy(pm_ctx* c) {
   if (c->ev_vel) cudaEventDestroy(c->ev_vel);
   c->row_cursor.release();
   c->scan_sums.release();
+  for (int i = 0; i < 2; ++i) { c->gspec[i].release(); c->ggrid[i].release(); }
+  c->d_sim3.release();
+  c->d_prefix3.release();
+  c->d_maps3.release();
   delete c;
 }
 
@@ -401,6 +466,7 @@ struct StepIO {
 // solve -> kick/drift in row order -> gathered back into particle order.
 int step_core(pm_ctx* c, const StepIO& io, long long np, double mass, double a, double da, float* rho_out,
               cudaStream_t st) {
+  const bool gradient = (c->cfg.flags & PM_FLAG_SPECTRAL_GRADIENT) != 0;
   const size_t gb = (size_t)c->n * c->n * c->n * sizeof(float);
   float* rho = rho_out;
   if (!rho) {
@@ -445,11 +511,13 @@ int step_core(pm_ctx* c, const StepIO& io, long long np, double mass, double a, 
                                c->row_start.as<unsigned>(), POS_ABS, c->d_err.as<int>(), c->tile_next.as<unsigned>(),
                                nullptr, grid_for(k.prefix[PH_DEP][1], c->sms, deposit_r2c_ctas_per_sm(c->n)), st),
           "fused deposit");
-    if (int r = spectral(c, k, false, st, true)) return r;
+    if (int r = spectral(c, k, false, st, true, gradient)) return r;
   } else {
     if (int r = deposit(c, k, nullptr, st)) return r;
-    if (int r = spectral(c, k, false, st)) return r;
+    if (int r = spectral(c, k, false, st, false, gradient)) return r;
   }
+  if (gradient)  // the kick's descriptor now names the three force grids
+    PM_CK(cudaMemcpyAsync(c->d_sim.p, &k.sim, sizeof(Sim), cudaMemcpyHostToDevice, st), "upload sim");
   if (io.vel_ready) PM_CK(cudaStreamWaitEvent(st, io.vel_ready, 0), "wait velocities");
   PM_CK(launch_gather_state(io.vel_in, nullptr, np, perm, c->svel.as<float>(), nullptr, c->sms, st), "gather");
   if (int r = kick(c, k, nullptr, st)) return r;

@@ -78,8 +78,10 @@ struct Plan {
 
 const int kStateArrays = 11;  // x y z vx vy vz id, cell record: cell fx fy fz
 
-// Schedules found by the autotuner, for the whole process: per (grid size, log2 of the size's
-// deposit tiles in the batch), and the kick's per log2 of its work units.
+// Schedules found by the autotuner, for the whole process: per (grid size, volume class of the
+// size's deposit tiles in the batch), and the kick's per volume class of its work units; a
+// class spans a factor 8 of work, so that a serving mix whose simulations come and go meets
+// few new classes.
 std::mutex g_tune_lock;
 std::map<std::pair<int, int>, Shape> g_shapes;
 std::map<int, int> g_kick_cps;
@@ -89,6 +91,8 @@ int ilog2(long long v) {
   while (v > 1) { v >>= 1; ++b; }
   return b;
 }
+
+int volume_class(long long units) { return ilog2(units > 1 ? units : 1) / 3; }
 
 }  // namespace
 
@@ -115,6 +119,7 @@ struct pm_batch {
   bool graphs = true;
   bool autotune = true;     // tune the schedule of new plans (see autotune)
   bool tuned = false;       // the current plan's schedule is settled
+  int plan_steps = 0;       // steps run since the plan was built
   bool sparse = false;      // the state the next step reads has empty slots (after a retirement)
   long long in_total = 0;   // slots of that state
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
@@ -132,7 +137,7 @@ struct pm_batch {
   size_t plan_host_bytes[2] = {0, 0};
   cudaEvent_t plan_ev[2] = {nullptr, nullptr};
   int plan_turn = 0;
-  double host_s[4] = {0, 0, 0, 0};  // host seconds: admission, planning, graph capture, retirement
+  double host_s[5] = {0, 0, 0, 0, 0};  // host seconds: admission, planning, graph capture, retirement, tuning
   std::string err;
 };
 
@@ -431,18 +436,19 @@ int build_plan(pm_batch* b, cudaStream_t st) {
     b->tuned = true;
     P.shape.assign(P.sizes.size(), Shape());
     for (size_t i = 0; i < P.sizes.size(); ++i) {
-      const auto key = std::make_pair(P.sizes[i], ilog2(std::max(1, P.fdep_total[i] ? P.fdep_total[i] : P.x_total[i])));
+      const auto key = std::make_pair(P.sizes[i], volume_class(P.fdep_total[i] ? P.fdep_total[i] : P.x_total[i]));
       auto it = g_shapes.find(key);
       if (it != g_shapes.end()) P.shape[i] = it->second;
       else b->tuned = false;
       if (!P.fused[i]) P.shape[i].dep = DEP_SEPARATE;
     }
-    auto kt = g_kick_cps.find(ilog2(std::max(1, P.fixed_total[PH_KICK])));
+    auto kt = g_kick_cps.find(volume_class(P.fixed_total[PH_KICK]));
     if (kt != g_kick_cps.end()) P.kick_cps = kt->second;
     else b->tuned = false;
   }
   drop_graphs(b);
   b->dirty = false;
+  b->plan_steps = 0;
   return PM_OK;
 }
 
@@ -566,18 +572,25 @@ int ensure_keys(pm_batch* b, cudaStream_t st) {
   return PM_OK;
 }
 
+// Steps a new plan runs (on the defaults or cached schedules) before it is tuned: the state of a
+// newly admitted simulation is in particle order until its first step has sorted it, and its
+// permutation reads are then scattered -- not the steady state that the timings must represent.
+constexpr int TUNE_AFTER_STEPS = 2;
+
 // Autotuner: for each grid size of the plan whose schedule is not in the process-wide cache,
 // and for the kick, time the candidate schedules on the batch's own data (one warm-up launch,
 // then the mean of three) and keep the fastest.  The candidates are the deposit modes (fused
-// with dense-first tiles, fused in index order, separate from the x R2C), the fused deposit's
-// CTAs per SM, the x passes' CTAs per SM and the kick's.  Runs between steps: the trials write
+// with dense-first tiles, or separate from the x R2C), the fused deposit's CTAs per SM, the x
+// passes' CTAs per SM and the kick's.  (Fused tiles in index order is not a candidate: it can
+// win on the even particle distribution of early steps, where it is timed, and then loses
+// badly once particles cluster -- 1.01 against 0.72 ms at step 980 of the 256^3 / 512^3 run.)  Runs between steps: the trials write
 // only buffers that the next step rewrites from scratch (spectra, grids, the next state, tile
 // counters) or scratch (the kick's keys and histogram go to unused sort buffers), never the
 // state the step reads or the histogram its sort consumes.
 int autotune(pm_batch* b, cudaStream_t st) {
   Plan& P = b->plan;
   if (b->tuned || !b->autotune) return PM_OK;
-  HostTimer timer(b->host_s[1]);
+  HostTimer timer(b->host_s[4]);
   const Sim* ds = b->d_sims.as<Sim>();
   int* err = b->d_err.as<int>();
   Parts in = state(b, b->cur), out = state(b, 1 - b->cur);
@@ -606,7 +619,7 @@ int autotune(pm_batch* b, cudaStream_t st) {
   std::vector<std::pair<std::pair<int, int>, Shape>> found;
   for (size_t g = 0; g < P.sizes.size() && !rc; ++g) {
     const int n = P.sizes[g];
-    const auto key = std::make_pair(n, ilog2(std::max(1, P.fdep_total[g] ? P.fdep_total[g] : P.x_total[g])));
+    const auto key = std::make_pair(n, volume_class(P.fdep_total[g] ? P.fdep_total[g] : P.x_total[g]));
     {
       std::lock_guard<std::mutex> lk(g_tune_lock);
       if (g_shapes.count(key)) continue;
@@ -617,7 +630,6 @@ int autotune(pm_batch* b, cudaStream_t st) {
       const int occ = deposit_r2c_ctas_per_sm(n);
       std::vector<Shape> cands;
       for (int cps = occ; cps >= 1; --cps) cands.push_back(Shape{DEP_FUSED_DENSE_FIRST, cps, best.x_cps});
-      cands.push_back(Shape{DEP_FUSED_INDEX, occ, best.x_cps});
       cands.push_back(Shape{DEP_SEPARATE, occ, best.x_cps});
       float best_ms = 1e30f;
       for (const Shape& c : cands) {
@@ -653,7 +665,7 @@ int autotune(pm_batch* b, cudaStream_t st) {
       found.emplace_back(key, best);
     }
   }
-  const int kkey = ilog2(std::max(1, P.fixed_total[PH_KICK]));
+  const int kkey = volume_class(P.fixed_total[PH_KICK]);
   bool kick_known;
   {
     std::lock_guard<std::mutex> lk(g_tune_lock);
@@ -967,8 +979,15 @@ int pm_batch_step(pm_batch* b, int nsteps, void* stream) {
     for (auto& s : b->sims) k = std::min(k, s->nsteps - s->done);
     if (k <= 0) break;
     if (int r = ensure_keys(b, st)) return r;
-    if (int r = autotune(b, st)) return r;
+    if (!b->tuned && b->autotune) {
+      if (b->plan_steps >= TUNE_AFTER_STEPS) {
+        if (int r = autotune(b, st)) return r;
+      } else {
+        k = std::min(k, TUNE_AFTER_STEPS - b->plan_steps);  // a sorted state first
+      }
+    }
     if (int r = run_steps(b, k, st)) return r;
+    b->plan_steps += k;
     for (auto& s : b->sims) {
       for (int i = 0; i < k; ++i) s->a += s->da;
       s->done += k;
@@ -1136,7 +1155,7 @@ int pm_batch_schedule(pm_batch* b, int* out, int cap) {
 
 int pm_batch_host_seconds(pm_batch* b, double* out, int n) {
   if (!b || !out || n < 0) return PM_ERR_ARG;
-  for (int i = 0; i < n && i < 4; ++i) out[i] = b->host_s[i];
+  for (int i = 0; i < n && i < 5; ++i) out[i] = b->host_s[i];
   return PM_OK;
 }
 
@@ -1153,7 +1172,8 @@ int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void*
   int k = nsteps;
   for (auto& s : b->sims) k = std::min(k, s->nsteps - s->done);
   if (int r = ensure_keys(b, st)) return r;
-  if (int r = autotune(b, st)) return r;
+  if (b->plan_steps >= TUNE_AFTER_STEPS)
+    if (int r = autotune(b, st)) return r;
   cudaEvent_t ev[PP_COUNT + 1];
   for (auto& e : ev) PB_CK(cudaEventCreate(&e), "event");
   int rc = PM_OK;
@@ -1162,6 +1182,7 @@ int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void*
     if (rc) break;
     b->cur = 1 - b->cur;
     compacted(b);
+    b->plan_steps += 1;
     for (auto& s : b->sims) { s->a += s->da; s->done += 1; }
     cudaError_t e = cudaEventSynchronize(ev[PP_COUNT]);
     if (e) { rc = bcuda(b, e, "profile sync"); break; }

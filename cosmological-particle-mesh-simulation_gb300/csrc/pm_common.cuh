@@ -92,6 +92,12 @@ struct Sim {
   const float2* tw;    // exp(-2 pi i m / n), m < n
   const int* q_int;    // lattice coordinate, integer part, np1 entries
   const float* q_frac; // lattice coordinate, fractional part, np1 entries
+  const float* sn;     // sin(2 pi m / n), m < n (spectral gradient)
+  // spectral gradient: grad_axis = d + 1 makes the z pass multiply by -i sin(k_d) as well as
+  // by the Green function, so that the inverse passes give the force grid of axis d; grad, for
+  // the kick, holds the three force grids (nullptr: central differences of phi)
+  int grad_axis, pad2;
+  const float* grad[3];
   // per-step coefficients
   float mass_scale;    // particle mass * 2^-PM_FIX_BITS
   float green;         // -3 Om / (8 a) / n^3
@@ -140,6 +146,7 @@ __device__ __forceinline__ void set_error(int* err, int code) {
 // spectral passes: one kernel per grid size n (supported n: spectral_supported)
 enum SpecKind : int { SPEC_X_R2C = 0, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Z_TABLE, SPEC_Y_INV, SPEC_X_C2R,
                       SPEC_Z_FWD, SPEC_Z_INV, /* plain z transforms (initial conditions) */
+                      SPEC_Z_GRAD, /* z Green times -i sin(k_d): spectral gradient of axis grad_axis - 1 */
                       SPEC_PREPARE /* only set kernel attributes */ };
 // maps: device array of tensor maps, two per simulation of `sims` (y pass, z pass; see
 // spectral_encode_maps) -- enables the TMA-streamed line passes; nullptr falls back to

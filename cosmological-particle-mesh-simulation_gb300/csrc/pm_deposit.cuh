@@ -182,19 +182,24 @@ __device__ __forceinline__ RunLoad run_load(const Sim& S, const unsigned* __rest
   return v;
 }
 
-// Warp-wide: the run table (first sorted index, and the inclusive scan of the counts).
-__device__ __forceinline__ void run_table(const RunLoad& v, int lane, unsigned* s_begin, unsigned* s_off) {
+// Warp-wide (all 32 lanes call it): the run table (first sorted index, and the inclusive scan
+// of the counts) of the tile whose runs the 8 lanes of this lane's group of eight loaded
+// (lane & 7 = the run).  The lanes with `write` store their group's table at s_begin / s_off.
+__device__ __forceinline__ void run_table(const RunLoad& v, int lane, unsigned* s_begin, unsigned* s_off,
+                                          bool write) {
+  const int r = lane & 7;
   unsigned incl = v.cnt;
 #pragma unroll
   for (int o = 1; o < 8; o <<= 1) {
-    const unsigned t = __shfl_up_sync(FULL, incl, o);
-    if (lane >= o) incl += t;
+    const unsigned t = __shfl_up_sync(FULL, incl, o, 8);
+    if (r >= o) incl += t;
   }
-  if (lane < NRUN) {
-    s_begin[lane] = v.beg;
-    s_off[lane + 1] = incl;
+  if (!write) return;
+  if (r < NRUN) {
+    s_begin[r] = v.beg;
+    s_off[r + 1] = incl;
   }
-  if (lane == 0) s_off[0] = 0;
+  if (r == 0) s_off[0] = 0;
 }
 
 // The particle loop of a tile: two source entries per lane and iteration, so that their
@@ -204,8 +209,8 @@ template <int MODE, int NT, bool ONE>
 __device__ __forceinline__ void deposit_sources(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
                                                 int* err, int y0, int z0, unsigned* lo, unsigned* hi, int rs,
                                                 const unsigned* s_begin, const unsigned* s_off, unsigned total,
-                                                float qscale) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                                                float qscale, int tid) {
+  const int lane = tid & 31, warp = tid >> 5;
   const int n = S.n;
   unsigned base = (unsigned)warp * 32u;
   unsigned sl0 = source_slot(perm, s_begin, s_off, base + lane, total);
@@ -226,24 +231,28 @@ __device__ __forceinline__ void deposit_sources(const Sim& S, const Parts& p, co
 // Accumulate the tile at (y0, z0) of simulation S into lo/hi: TZ * TY rows of n cells, row r
 // of lo at word r * rs and of hi at the same offset from hi (hi is only written by two-word
 // tiles).  s_begin / s_off: NRUN + 1 words each, already holding the tile's run table when
-// runs_ready.  Entered and left by all NT threads, synchronised.  Returns how the sums are
-// held (tile_sum).
+// runs_ready.  Done by NT threads, tid = 0 .. NT - 1 (a whole CTA, or a group of its warps
+// with one tile each: every group calls it together, it synchronises the whole CTA).  Returns
+// how the sums are held (tile_sum), also written to *ts_out when given.
 template <int MODE, int NT>
 __device__ __forceinline__ TileSum deposit_tile(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
                                                 const unsigned* __restrict__ row_start, int* err, int y0, int z0,
                                                 unsigned* lo, unsigned* hi, int rs, unsigned* s_begin,
-                                                unsigned* s_off, bool runs_ready = false) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                                                unsigned* s_off, bool runs_ready = false, int tid = -1,
+                                                TileSum* ts_out = nullptr) {
+  if (tid < 0) tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
   const int n = S.n;
   if (!runs_ready) {
-    if (warp == 0) run_table(run_load(S, row_start, y0, z0, lane), lane, s_begin, s_off);
+    if (warp == 0) run_table(run_load(S, row_start, y0, z0, lane), lane, s_begin, s_off, lane < 8);
     __syncthreads();
   }
   const unsigned total = s_off[NRUN];
   const TileSum ts = tile_sum(total, S.mass_scale);
+  if (ts_out && tid == 0) *ts_out = ts;  // visible to the whole CTA after the barrier below
   // zero the rows of lo (and of hi for two-word sums), 4 words per store
   const int q4 = n / 4;
-  for (int i = threadIdx.x; i < TZ * TY * q4; i += NT) {
+  for (int i = tid; i < TZ * TY * q4; i += NT) {
     const int off = (i / q4) * rs + (i % q4) * 4;
     *reinterpret_cast<uint4*>(lo + off) = make_uint4(0u, 0u, 0u, 0u);
     if (!ts.s) *reinterpret_cast<uint4*>(hi + off) = make_uint4(0u, 0u, 0u, 0u);
@@ -251,10 +260,10 @@ __device__ __forceinline__ TileSum deposit_tile(const Sim& S, const Parts& p, co
   __syncthreads();
   if (ts.s)
     deposit_sources<MODE, NT, true>(S, p, perm, err, y0, z0, lo, hi, rs, s_begin, s_off, total,
-                                    __uint_as_float((unsigned)(127 + ts.s) << 23));
+                                    __uint_as_float((unsigned)(127 + ts.s) << 23), tid);
   else
     deposit_sources<MODE, NT, false>(S, p, perm, err, y0, z0, lo, hi, rs, s_begin, s_off, total,
-                                     (float)(1u << PM_FIX_BITS));
+                                     (float)(1u << PM_FIX_BITS), tid);
   __syncthreads();
   return ts;
 }

@@ -52,29 +52,33 @@ struct DBuf {
   template <typename T> T* as() const { return static_cast<T*>(p); }
 };
 
-// Per-grid-size tables: s2[m] = sin^2(pi m / n) (fourier_utils.py:9-15 per axis) and
-// tw[m] = exp(-2 pi i m / n), both built in double precision on the host.
+// Per-grid-size tables: s2[m] = sin^2(pi m / n) (fourier_utils.py:9-15 per axis),
+// sn[m] = sin(2 pi m / n) (the spectral central difference) and tw[m] = exp(-2 pi i m / n),
+// built in double precision on the host.
 struct Tables {
   int n = 0;
-  DBuf s2, tw;
+  DBuf s2, tw, sn;
   cudaError_t build(int nn) {
     if (n == nn && s2.p) return cudaSuccess;
-    std::vector<float> hs(nn);
+    std::vector<float> hs(nn), hn(nn);
     std::vector<float2> ht(nn);
     for (int m = 0; m < nn; ++m) {
       const double s = std::sin(M_PI * (double)m / nn);
       hs[m] = (float)(s * s);
+      hn[m] = (float)std::sin(2.0 * M_PI * (double)m / nn);
       const double ang = -2.0 * M_PI * (double)m / nn;
       ht[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
     }
     cudaError_t e = s2.ensure(nn * sizeof(float));
     if (!e) e = tw.ensure(nn * sizeof(float2));
+    if (!e) e = sn.ensure(nn * sizeof(float));
+    if (!e) e = cudaMemcpy(sn.p, hn.data(), nn * sizeof(float), cudaMemcpyHostToDevice);
     if (!e) e = cudaMemcpy(s2.p, hs.data(), nn * sizeof(float), cudaMemcpyHostToDevice);
     if (!e) e = cudaMemcpy(tw.p, ht.data(), nn * sizeof(float2), cudaMemcpyHostToDevice);
     if (!e) n = nn;
     return e;
   }
-  void release() { s2.release(); tw.release(); n = 0; }
+  void release() { s2.release(); tw.release(); sn.release(); n = 0; }
 };
 
 // Lagrangian lattice of one axis: q = i * (n_cells / n_parts) + 0.5 (zeldovich.py:79-83),

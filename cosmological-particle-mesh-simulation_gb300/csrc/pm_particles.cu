@@ -190,6 +190,26 @@ __device__ __forceinline__ void gather_force(const float* __restrict__ phi, int 
   gather_taps(GlobalRows(phi, n, c.y, c.z), n, c, g);
 }
 
+// The same force from the three force grids of the spectral gradient (each already the halved
+// central difference, -i sin(k_d) phi_k transformed back): 8 taps per axis at the CIC corners,
+// combined with the weights in the order of integrate.py:92.
+__device__ __forceinline__ void gather_grad(const Sim& S, const Cell& c, float g[3]) {
+  float w[8];
+  cic_weights(c, w);
+  const int n = S.n;
+  const int x0 = c.x, x1 = c.x + 1 == n ? 0 : c.x + 1;
+  const int y1 = c.y + 1 == n ? 0 : c.y + 1, z1 = c.z + 1 == n ? 0 : c.z + 1;
+  const size_t r00 = ((size_t)c.z * n + c.y) * n, r10 = ((size_t)c.z * n + y1) * n;
+  const size_t r01 = ((size_t)z1 * n + c.y) * n, r11 = ((size_t)z1 * n + y1) * n;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float* __restrict__ G = S.grad[d];
+    g[d] = __ldg(&G[r00 + x0]) * w[0] + __ldg(&G[r00 + x1]) * w[1] + __ldg(&G[r10 + x0]) * w[2] +
+           __ldg(&G[r01 + x0]) * w[3] + __ldg(&G[r10 + x1]) * w[4] + __ldg(&G[r01 + x1]) * w[5] +
+           __ldg(&G[r11 + x0]) * w[6] + __ldg(&G[r11 + x1]) * w[7];
+  }
+}
+
 // Kick/drift of one particle whose state and force are in registers; writes it out and
 // returns its next key (resident mode with keys_next; else 0xffffffff).
 template <int MODE>
@@ -266,7 +286,10 @@ __global__ void __launch_bounds__(KICK_NT, 4) k_kick(const Sim* __restrict__ sim
 #pragma unroll
     for (int q = 0; q < KICK_PPT; ++q) {
       g[q][0] = g[q][1] = g[q][2] = 0.f;
-      if (slot[q] >= 0 && c[q].ok) gather_force(S.phi, S.n, c[q], g[q]);
+      if (slot[q] >= 0 && c[q].ok) {
+        if (S.grad[0]) gather_grad(S, c[q], g[q]);  // spectral gradient: three force grids
+        else gather_force(S.phi, S.n, c[q], g[q]);
+      }
     }
     unsigned key[KICK_PPT];
 #pragma unroll

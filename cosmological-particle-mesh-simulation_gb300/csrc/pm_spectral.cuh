@@ -311,7 +311,8 @@ __global__ void __launch_bounds__(SP_NT) k_line_pass(const Sim* __restrict__ sim
 
 // Green function of potential.py:15 / fourier_utils.py:15-16 (k = 0 -> 0), including
 // the 1/n^3 of the unnormalised inverse transforms (folded into S.green).
-template <int N, bool TABLE>
+// GRAD: the spectral gradient of axis S.grad_axis - 1 as well (times -i sin(k_d)).
+template <int N, bool TABLE, bool GRAD>
 __device__ __forceinline__ void z_body(const Sim& S, int unit, float2* s) {
   constexpr int BW = cline_width(N), BPC = cline_bpc(N), NL = BW * BPC;
   constexpr int NBP = cbundles_per_plane(N), W = chalf(N);
@@ -335,20 +336,26 @@ __device__ __forceinline__ void z_body(const Sim& S, int unit, float2* s) {
       }
     }
     const float2 v = s[e];
-    s[e] = make_float2(v.x * g, v.y * g);
+    if (GRAD) {  // times -i sin(k_d): the spectral central difference along axis d
+      const float sg =
+          kx < W && ky < N ? g * __ldg(&S.sn[S.grad_axis == 1 ? kx : (S.grad_axis == 2 ? ky : kz)]) : 0.f;
+      s[e] = make_float2(sg * v.y, -sg * v.x);
+    } else {
+      s[e] = make_float2(v.x * g, v.y * g);
+    }
   }
   __syncthreads();
   fft_lines<N, NL, NL, SP_NT, true>(s, S.tw, 1);
   store_bundles<N, true>(S, unit, s);
 }
 
-template <int N, bool TABLE>
+template <int N, bool TABLE, bool GRAD = false>
 __global__ void __launch_bounds__(SP_NT) k_z_green(const Sim* __restrict__ sims, Work w) {
   extern __shared__ float4 smem_f4[];
   float2* s = reinterpret_cast<float2*>(smem_f4);
   for (int unit = blockIdx.x; unit < w.total; unit += gridDim.x) {
     const int si = locate_sim(w, unit);
-    z_body<N, TABLE>(sims[si], unit - __ldg(&w.prefix[si]), s);
+    z_body<N, TABLE, GRAD>(sims[si], unit - __ldg(&w.prefix[si]), s);
     __syncthreads();
   }
 }
@@ -367,12 +374,14 @@ __global__ void __launch_bounds__(SP_NT) k_z_green(const Sim* __restrict__ sims,
 // Green function of potential.py:15 / fourier_utils.py:15-16 (k = 0 -> 0; the 1/n^3 of the
 // unnormalised inverse transforms is folded into g0) for element kz of line `line` of a unit
 // of the z pass whose first bundle is b0.
-template <int N, bool TABLE>
+template <int N, bool TABLE, bool GRAD = false>
 struct GreenEpi {
   float g0;
   const float* s2;
   const float* fgrid;
   int b0, cnt;
+  const float* sn;  // GRAD, the spectral gradient of axis grad_axis - 1: times -i sin(k_d) as well
+  int grad_axis;
   __device__ __forceinline__ float2 operator()(float2 v, int kz, int line) const {
     constexpr int BW = cline_width(N), NBP = cbundles_per_plane(N), W = chalf(N);
     const int i = line / BW, b = b0 + i;
@@ -382,11 +391,16 @@ struct GreenEpi {
       if (TABLE) g = g0 * __ldg(&fgrid[((long long)kz * N + ky) * N + kx]);
       else if ((kx | ky | kz) != 0) g = __fdividef(g0, __ldg(&s2[kx]) + __ldg(&s2[ky]) + __ldg(&s2[kz]));
     }
+    if (GRAD) {
+      const float sg = i < cnt && kx < W ? g * __ldg(&sn[grad_axis == 1 ? kx : (grad_axis == 2 ? ky : kz)]) : 0.f;
+      return make_float2(sg * v.y, -sg * v.x);
+    }
     return make_float2(v.x * g, v.y * g);
   }
 };
 
-// MODE 0: y forward, 1: y inverse, 2: z Green, 3: z Green (caller table), 4: z forward, 5: z inverse
+// MODE 0: y forward, 1: y inverse, 2: z Green, 3: z Green (caller table), 4: z forward, 5: z inverse,
+// 6: z Green times -i sin(k_d) (spectral gradient of axis S.grad_axis - 1)
 template <int N, int MODE>
 __global__ void __launch_bounds__(line_nt(N), line_ctas_per_sm(N)) k_line_tma(const CUtensorMap* __restrict__ maps,
                                                         const Sim* __restrict__ sims, Work w, int* err) {
@@ -457,7 +471,7 @@ __global__ void __launch_bounds__(line_nt(N), line_ctas_per_sm(N)) k_line_tma(co
       fft_lines_blocked<N, NL, BW, line_nt(N), true>(s, S.tw, 1);
     } else {
       // forward z transform, the Green function, inverse z transform (meeting in registers)
-      const GreenEpi<N, MODE == 3> epi{S.green, S.s2, S.fgrid, b0, cnt};
+      const GreenEpi<N, MODE == 3, MODE == 6> epi{S.green, S.s2, S.fgrid, b0, cnt, S.sn, S.grad_axis};
       fft_lines_blocked_turn<N, NL, BW, line_nt(N)>(s, S.tw, 1, epi);
     }
     fence_proxy_async_smem();
@@ -753,6 +767,16 @@ __host__ __device__ constexpr int deposit_r2c_nt(int n) { return xrow_ok(n) ? DE
 // sizes whose tile (TZ * TY rows of n cells) divides evenly over the block
 __host__ __device__ constexpr bool deposit_r2c_ok(int n) { return (TZ * TY * n) % deposit_r2c_nt(n) == 0; }
 
+// Tiles per CTA of the fused deposit: the register row transform of a tile's 16 rows keeps
+// 16 / T warps busy (T lanes per row), so on the sizes with T < 16 a CTA takes several tiles
+// at once -- its warps split into one group per tile for the particle loop and share all the
+// rows in the transform -- as long as their accumulators stay within 72 KB (three CTAs per SM).
+__host__ __device__ constexpr int dep_tiles(int n) {
+  int t = xrow_ok(n) ? 16 / xrow_T(n) : 1;
+  while (t > 1 && (size_t)t * deposit_r2c_smem_bytes(n) > 72 * 1024) t /= 2;
+  return t;
+}
+
 template <int N, int MODE>
 __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
     k_deposit_r2c(const Sim* __restrict__ sims, Work w, Parts p, const unsigned* __restrict__ perm,
@@ -761,50 +785,83 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
   constexpr int NT = deposit_r2c_nt(N);
   constexpr int M = N / 2, NL = TZ * TY, LS = NL + 1;
   constexpr int PER = NL * N / NT;
+  constexpr int TPB = dep_tiles(N);  // tiles per CTA
   static_assert(NL * N % NT == 0, "tile cells must divide by the block size");
   static_assert((size_t)M * LS * sizeof(float2) <= deposit_r2c_smem_bytes(N), "FFT buffer must fit");
+  static_assert(TPB * 8 <= 32 && NT % (TPB * 32) == 0, "one warp loads the run tables of a CTA's tiles");
   extern __shared__ uint4 acc_raw[];
-  __shared__ unsigned s_begin[NSRC];
-  __shared__ unsigned s_off[NSRC + 1];
+  // run tables of the CTA's tiles (7 runs each: first sorted index, and inclusive offsets)
+  __shared__ unsigned s_begin[TPB][8];
+  __shared__ unsigned s_off[TPB][8];
+  __shared__ TileSum s_ts[TPB];
   unsigned* lo = reinterpret_cast<unsigned*>(acc_raw);
-  // row r: lo at r * RS, hi at r * RS + HO
+  // row r: lo at r * RS, hi at r * RS + HO (tiles one after another, NL rows each)
   constexpr int RS = xrow_ok(N) ? 2 * N : N, HO = xrow_ok(N) ? N : NL * N;
   unsigned* hi = lo + HO;
   float2* F = reinterpret_cast<float2*>(acc_raw);
   float* Ff = reinterpret_cast<float*>(acc_raw);
-  bool runs_ready = false;  // the run table of this tile was loaded during the previous one
-  // Tiles are taken from a counter (zero at launch) after the first, one per CTA: a tile's
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // Tiles are taken from a counter (zero at launch) after the first, TPB per CTA: a tile's
   // work is its particle count, which clustering makes very uneven, so a fixed stride
   // leaves the CTAs that drew the dense tiles running alone at the end.
   // `order` (optional) lists the tiles dense-first; idx is the place in it.
   __shared__ int s_next;
   auto take_next = [&](int idx) -> int {
-    return next_tile ? (int)gridDim.x + (int)atomicAdd(next_tile, 1u) : idx + (int)gridDim.x;
+    return next_tile ? (int)gridDim.x * TPB + (int)atomicAdd(next_tile, (unsigned)TPB) : idx + (int)gridDim.x * TPB;
   };
   auto tile_at = [&](int idx) -> int { return order ? (int)__ldg(&order[idx]) : idx; };
-  for (int idx = blockIdx.x; idx < w.total;) {
-    const int unit = tile_at(idx);
-    const int si = locate_sim(w, unit);
-    const Sim& S = sims[si];
+  // the tile at place i of the order: its simulation and first row / plane (false: none)
+  auto tile_of = [&](int i, int& si, int& y0, int& z0) -> bool {
+    si = 0; y0 = z0 = 0;
+    if (i >= w.total) return false;
+    const int unit = tile_at(i);
+    si = locate_sim(w, unit);
     const int local = unit - __ldg(&w.prefix[si]);
-    const int y0 = (local % (N / TY)) * TY, z0 = (local / (N / TY)) * TZ;
-    const TileSum ts = deposit_tile<MODE, NT>(S, p, perm, row_start, err, y0, z0, lo, hi, RS, s_begin, s_off,
-                                              runs_ready);
-    runs_ready = false;
-    if constexpr (xrow_ok(N)) {
-      // the tile's NL rows: T lanes per row, rows r = warp * RPW + sub; the row's exchange
+    y0 = (local % (N / TY)) * TY;
+    z0 = (local / (N / TY)) * TZ;
+    return true;
+  };
+  if constexpr (xrow_ok(N)) {
+    constexpr int NTT = NT / TPB;  // threads per tile group
+    constexpr int P = xrow_P(N), Q = xrow_Q(N), T = xrow_T(N), RPW = 32 / T;
+    constexpr int NB1 = Q / T, NB2 = P / T;
+    static_assert(Q * (P + 1) * sizeof(float2) <= 2 * N * sizeof(unsigned), "exchange buffer in the row");
+    const int g = threadIdx.x / NTT, gtid = threadIdx.x % NTT;
+    // warp 0: the run tables of the tiles at places idx .. idx + TPB - 1 (8 lanes per tile)
+    auto load_tables = [&](int idx) -> RunLoad {
+      RunLoad v{0u, 0u};
+      int si, y0, z0;
+      if (tile_of(idx + (lane >> 3), si, y0, z0)) v = run_load(sims[si], row_start, y0, z0, lane & 7);
+      return v;
+    };
+    int idx = blockIdx.x * TPB;
+    if (warp == 0 && idx < w.total) {
+      const RunLoad v = load_tables(idx);
+      const int tj = lane < TPB * 8 ? lane >> 3 : 0;
+      run_table(v, lane, s_begin[tj], s_off[tj], lane < TPB * 8);
+    }
+    __syncthreads();
+    while (idx < w.total) {
+      {  // the particles of this group's tile (a group without a tile has an empty table)
+        int si, y0, z0;
+        tile_of(idx + g, si, y0, z0);
+        deposit_tile<MODE, NTT>(sims[si], p, perm, row_start, err, y0, z0, lo + g * NL * RS, hi + g * NL * RS, RS,
+                                s_begin[g], s_off[g], true, gtid, &s_ts[g]);
+      }
+      // the CTA's TPB * NL rows: T lanes per row, rows R = warp * RPW + sub; a row's exchange
       // buffer overlays its own accumulator words once they are read
-      constexpr int P = xrow_P(N), Q = xrow_Q(N), T = xrow_T(N), RPW = 32 / T;
-      constexpr int NB1 = Q / T, NB2 = P / T;
-      static_assert(Q * (P + 1) * sizeof(float2) <= 2 * N * sizeof(unsigned), "exchange buffer in the row");
-      const int lane = threadIdx.x & 31, sub = lane / T, t = lane % T;
-      const int r = (threadIdx.x >> 5) * RPW + sub;
-      float2* rb = reinterpret_cast<float2*>(lo + r * RS);
-      if ((threadIdx.x >> 5) * RPW < NL) {  // warp-uniform
+      const int sub = lane / T, t = lane % T;
+      const int R = warp * RPW + sub, tg = R / NL, r = R % NL;
+      float2* rb = reinterpret_cast<float2*>(lo + R * RS);
+      if (warp * RPW < TPB * NL) {  // warp-uniform
+        int tsi, ty0, tz0;
+        const bool thas = tile_of(idx + tg, tsi, ty0, tz0);
+        const Sim& S = sims[tsi];
+        const TileSum ts = s_ts[tg];
         float2 v2[NB1][P];
         float2 o2[NB2][Q];
-        const uint2* l2 = reinterpret_cast<const uint2*>(lo + r * RS);
-        const uint2* h2 = reinterpret_cast<const uint2*>(lo + r * RS + HO);
+        const uint2* l2 = reinterpret_cast<const uint2*>(lo + R * RS);
+        const uint2* h2 = reinterpret_cast<const uint2*>(lo + R * RS + HO);
 #pragma unroll
         for (int i = 0; i < NB1; ++i)
 #pragma unroll
@@ -813,61 +870,67 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
             const uint2 ll = l2[j], hh = ts.s ? make_uint2(0u, 0u) : h2[j];
             v2[i][a] = make_float2(sum_to_float(ts, ll.x, hh.x), sum_to_float(ts, ll.y, hh.y));
           }
-        // warp 0 takes the next tile and loads its run table now, and stores it after the
-        // transform, so that the loads' latency hides behind it (the table is free: the
-        // particle loop of this tile is over)
+        // warp 0 takes the next tiles and loads their run tables now, and stores them after the
+        // transform, so that the loads' latency hides behind it (the tables are free: the
+        // particle loops are over, and the transform reads s_ts)
         int next = 0;
-        if (threadIdx.x < 32) next = __shfl_sync(FULL, lane == 0 ? take_next(idx) : 0, 0);
+        if (warp == 0) next = __shfl_sync(FULL, lane == 0 ? take_next(idx) : 0, 0);
         RunLoad nl{0u, 0u};
-        int nsi = 0, ny0 = 0, nz0 = 0;
-        if (threadIdx.x < 32 && next < w.total) {
-          const int nunit = tile_at(next);
-          nsi = locate_sim(w, nunit);
-          const int nloc = nunit - __ldg(&w.prefix[nsi]);
-          ny0 = (nloc % (N / TY)) * TY;
-          nz0 = (nloc / (N / TY)) * TZ;
-          nl = run_load(sims[nsi], row_start, ny0, nz0, lane);
-        }
+        if (warp == 0 && next < w.total) nl = load_tables(next);
         xrow_transform<N, false>(v2, o2, rb, t, S.tw);
-        const long long row = (long long)(z0 + r / TY) * N + (y0 + r % TY);
-        xrow_untangle_store<N>(o2, rb, t, S.tw, S.spec + row * S.pitch);
-        if (threadIdx.x < 32 && next < w.total) run_table(nl, lane, s_begin, s_off);
+        if (thas) {
+          const long long row = (long long)(tz0 + r / TY) * N + (ty0 + r % TY);
+          xrow_untangle_store<N>(o2, rb, t, S.tw, S.spec + row * S.pitch);
+        }
+        if (warp == 0 && next < w.total) {
+          const int tj = lane < TPB * 8 ? lane >> 3 : 0;
+          run_table(nl, lane, s_begin[tj], s_off[tj], lane < TPB * 8);
+        }
         if (threadIdx.x == 0) s_next = next;
       }
       __syncthreads();
-      runs_ready = true;
       idx = s_next;
-      continue;
     }
-    float v[PER];
+    return;
+  } else {
+    bool runs_ready = false;
+    for (int idx = blockIdx.x; idx < w.total;) {
+      int si, y0, z0;
+      tile_of(idx, si, y0, z0);
+      const Sim& S = sims[si];
+      const TileSum ts = deposit_tile<MODE, NT>(S, p, perm, row_start, err, y0, z0, lo, hi, RS, s_begin[0], s_off[0],
+                                                runs_ready);
+      runs_ready = false;
+      float v[PER];
 #pragma unroll
-    for (int k = 0; k < PER; ++k) {
-      const int i = threadIdx.x + k * NT;
-      v[k] = sum_to_float(ts, lo[i], ts.s ? 0u : hi[i]);
-    }
-    __syncthreads();
+      for (int k = 0; k < PER; ++k) {
+        const int i = threadIdx.x + k * NT;
+        v[k] = sum_to_float(ts, lo[i], ts.s ? 0u : hi[i]);
+      }
+      __syncthreads();
 #pragma unroll
-    for (int k = 0; k < PER; ++k) {
-      const int i = threadIdx.x + k * NT;
-      const int r = i / N, x = i % N;
-      Ff[((x >> 1) * LS + r) * 2 + (x & 1)] = v[k];  // z[j] = x[2j] + i x[2j+1] of row r
+      for (int k = 0; k < PER; ++k) {
+        const int i = threadIdx.x + k * NT;
+        const int r = i / N, x = i % N;
+        Ff[((x >> 1) * LS + r) * 2 + (x & 1)] = v[k];  // z[j] = x[2j] + i x[2j+1] of row r
+      }
+      __syncthreads();
+      fft_lines<M, NL, LS, NT, false>(F, S.tw, 2);
+      float2* __restrict__ dst = S.spec;
+      const int P = S.pitch;
+      for (int u = threadIdx.x; u < NL * (M + 1); u += NT) {
+        const int r = u / (M + 1), k = u % (M + 1);
+        const long long row = (long long)(z0 + r / TY) * N + (y0 + r % TY);
+        const float2 zk = F[(k == M ? 0 : k) * LS + r];
+        const float2 zc = conjf2(F[(k == 0 ? 0 : M - k) * LS + r]);
+        const float2 e = cscale(cadd(zk, zc), 0.5f);
+        const float2 o = cscale(mul_mi<false>(csub(zk, zc)), 0.5f);
+        dst[row * P + k] = cadd(e, cmul(__ldg(&S.tw[k]), o));
+      }
+      if (threadIdx.x == 0) s_next = take_next(idx);
+      __syncthreads();
+      idx = s_next;
     }
-    __syncthreads();
-    fft_lines<M, NL, LS, NT, false>(F, S.tw, 2);
-    float2* __restrict__ dst = S.spec;
-    const int P = S.pitch;
-    for (int u = threadIdx.x; u < NL * (M + 1); u += NT) {
-      const int r = u / (M + 1), k = u % (M + 1);
-      const long long row = (long long)(z0 + r / TY) * N + (y0 + r % TY);
-      const float2 zk = F[(k == M ? 0 : k) * LS + r];
-      const float2 zc = conjf2(F[(k == 0 ? 0 : M - k) * LS + r]);
-      const float2 e = cscale(cadd(zk, zc), 0.5f);
-      const float2 o = cscale(mul_mi<false>(csub(zk, zc)), 0.5f);
-      dst[row * P + k] = cadd(e, cmul(__ldg(&S.tw[k]), o));
-    }
-    if (threadIdx.x == 0) s_next = take_next(idx);
-    __syncthreads();
-    idx = s_next;
   }
 }
 
@@ -879,7 +942,7 @@ cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned*
     return cudaErrorNotSupported;
   } else {
   static DeviceOnce once;
-  const size_t sm = deposit_r2c_smem_bytes(N);
+  const size_t sm = dep_tiles(N) * deposit_r2c_smem_bytes(N);
   const cudaError_t ie = once.run([&]() {
     cudaError_t e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_ABS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (!e) e = cudaFuncSetAttribute(k_deposit_r2c<N, POS_DISP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -889,7 +952,9 @@ cudaError_t deposit_r2c_launch(const Sim* sims, Work w, Parts p, const unsigned*
   });
   if (ie) return ie;
   if (ctas <= 0) return cudaSuccess;  // attribute setup only
-  constexpr int NT = deposit_r2c_nt(N);
+  constexpr int NT = deposit_r2c_nt(N), TPB = dep_tiles(N);
+  if (ctas > (w.total + TPB - 1) / TPB) ctas = (w.total + TPB - 1) / TPB;  // TPB tiles per CTA
+  if (ctas <= 0) return cudaSuccess;
   if (next_tile) {
     const cudaError_t e = cudaMemsetAsync(next_tile, 0, sizeof(unsigned), st);
     if (e) return e;
@@ -927,6 +992,7 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
       if (!e) e = max_shared(k_line_tma<N, 3>, tma_smem_bytes(N));
       if (!e) e = max_shared(k_line_tma<N, 4>, tma_smem_bytes(N));
       if (!e) e = max_shared(k_line_tma<N, 5>, tma_smem_bytes(N));
+      if (!e) e = max_shared(k_line_tma<N, 6>, tma_smem_bytes(N));
       if (e) return e;
     }
     cudaError_t e = max_shared(k_x_r2c<N>, xs);
@@ -937,6 +1003,7 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
     if (!e) e = max_shared(k_line_pass<N, true, true>, ls);
     if (!e) e = max_shared(k_z_green<N, false>, ls);
     if (!e) e = max_shared(k_z_green<N, true>, ls);
+    if (!e) e = max_shared(k_z_green<N, false, true>, ls);
     return e;
   });
   if (ie) return ie;
@@ -971,6 +1038,7 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
         case SPEC_Z_TABLE: k_line_tma<N, 3><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
         case SPEC_Z_FWD: k_line_tma<N, 4><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
         case SPEC_Z_INV: k_line_tma<N, 5><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
+        case SPEC_Z_GRAD: k_line_tma<N, 6><<<grid, line_nt(N), sm, st>>>(maps, sims, w, err); return cudaGetLastError();
         default: break;
       }
     }
@@ -984,6 +1052,7 @@ cudaError_t spectral_launch(SpecKind kind, const Sim* sims, Work w, int ctas, cu
     case SPEC_Z_INV: k_line_pass<N, true, true><<<ctas, SP_NT, ls, st>>>(sims, w); break;
     case SPEC_Z_GREEN: k_z_green<N, false><<<ctas, SP_NT, ls, st>>>(sims, w); break;
     case SPEC_Z_TABLE: k_z_green<N, true><<<ctas, SP_NT, ls, st>>>(sims, w); break;
+    case SPEC_Z_GRAD: k_z_green<N, false, true><<<ctas, SP_NT, ls, st>>>(sims, w); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

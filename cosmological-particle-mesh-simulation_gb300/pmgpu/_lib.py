@@ -15,6 +15,7 @@ P_double = ctypes.POINTER(ctypes.c_double)
 PM_OK, PM_ERR_ARG, PM_ERR_CUDA, PM_ERR_OOM, PM_ERR_DEVICE, PM_ERR_ADMIT = range(6)
 PM_FLAG_FIX_COSMO_F = 1
 PM_FLAG_KEEP_DENSITY = 2
+PM_FLAG_SPECTRAL_GRADIENT = 4
 DEVICE_BITS = {1: "cell out of range / non-finite position", 2: "particle outside its deposit tile",
                4: "non-finite kick/drift result"}
 

@@ -152,10 +152,10 @@ class Batch:
         return out
 
     def host_seconds(self) -> dict:
-        """Host time spent so far in admissions, planning, graph capture and retirements."""
-        arr = (ctypes.c_double * 4)()
-        self._check(self._lib.pm_batch_host_seconds(self._h, arr, 4))
-        return dict(zip(("admit", "plan", "capture", "retire"), [round(float(x), 4) for x in arr]))
+        """Host time spent so far in admissions, planning, graph capture, retirements and tuning."""
+        arr = (ctypes.c_double * 5)()
+        self._check(self._lib.pm_batch_host_seconds(self._h, arr, 5))
+        return dict(zip(("admit", "plan", "capture", "retire", "tune"), [round(float(x), 4) for x in arr]))
 
     def launches_per_step(self) -> int:
         return int(self._lib.pm_batch_launches_per_step(self._h))

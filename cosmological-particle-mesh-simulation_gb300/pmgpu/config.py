@@ -3,7 +3,7 @@ from __future__ import annotations
 
 import dataclasses
 
-from ._lib import PM_FLAG_FIX_COSMO_F, PM_FLAG_KEEP_DENSITY, PMConfigC
+from ._lib import PM_FLAG_FIX_COSMO_F, PM_FLAG_KEEP_DENSITY, PM_FLAG_SPECTRAL_GRADIENT, PMConfigC
 
 
 @dataclasses.dataclass
@@ -27,6 +27,7 @@ class Config:
     a_end: float = 1.0          # A_END
     fix_cosmo_f: bool = False   # evaluate f(a) with Omega_m in its slot (reference passes H0)
     keep_density: bool = False  # batch engine: keep the density grid apart from the potential
+    spectral_gradient: bool = False  # drop-in step: force from -i sin(k) phi_k grids, not 32 taps
 
     @property
     def mass(self) -> float:
@@ -44,7 +45,8 @@ class Config:
 
     def c_struct(self) -> PMConfigC:
         flags = (PM_FLAG_FIX_COSMO_F if self.fix_cosmo_f else 0) | (
-            PM_FLAG_KEEP_DENSITY if self.keep_density else 0)
+            PM_FLAG_KEEP_DENSITY if self.keep_density else 0) | (
+            PM_FLAG_SPECTRAL_GRADIENT if self.spectral_gradient else 0)
         return PMConfigC(self.n_cells, self.n_parts, float(self.box_size), self.omega_m0, self.omega_b0,
                          self.omega_k0, self.omega_lambda0, self.h0, self.a_init, self.a_end, self.steps,
                          flags)

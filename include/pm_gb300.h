@@ -41,6 +41,10 @@ extern "C" {
 #define PM_FLAG_FIX_COSMO_F 1  /* f(a) with Omega_m in its slot; the reference passes H0
                                   there (src/integrate.py:12) and is followed by default */
 #define PM_FLAG_KEEP_DENSITY 2 /* batch: keep the density grid apart from the potential */
+#define PM_FLAG_SPECTRAL_GRADIENT 4 /* pm_step / pm_step_host: the force from three force grids,
+                                       -i sin(k_d) phi_k transformed back (the spectral form of
+                                       the central difference of src/integrate.py:84-92, equal
+                                       up to rounding), instead of 32 potential taps */
 
 /* Mirrors src/configure_me.py:7-40 (plotting / saving switches omitted). */
 typedef struct pm_config {
@@ -209,9 +213,8 @@ int pm_batch_profile(pm_batch* b, int nsteps, float* phase_ms, int nphase, void*
 /* Kernel launches per step for the resident simulations (-1 on error). */
 int pm_batch_launches_per_step(pm_batch* b);
 /* The launch schedule of each grid size is tuned on the batch's own data when a plan meets a
-   size (and work volume) it has not timed before in this process: deposit fused with the x
-   R2C (dense tiles first or in index order) or separate, CTAs per SM of the fused deposit, of
-   the x passes and of the kick.  Every candidate gives bit-identical results.  enable = 0 keeps
+   size (and class of work volume) it has not timed before in this process: deposit fused with
+   the x R2C or separate, CTAs per SM of the fused deposit, of the x passes and of the kick.  Every candidate gives bit-identical results.  enable = 0 keeps
    the defaults (and schedules already tuned).  No counterpart in the reference: its FFTs are
    planned by FFTW (src/potential.py:20,27). */
 int pm_batch_set_autotune(pm_batch* b, int enable);
@@ -219,8 +222,8 @@ int pm_batch_set_autotune(pm_batch* b, int enable);
    1 fused index order / 2 separate, fused-deposit CTAs per SM, x-pass CTAs per SM), then
    (0, kick CTAs per SM, 1 if tuned, 0).  Returns the ints written (-1 on error). */
 int pm_batch_schedule(pm_batch* b, int* out, int cap);
-/* Host seconds the batch has spent so far (out[0..n-1], n <= 4): admissions, planning, CUDA
-   graph capture and instantiation, retirements. */
+/* Host seconds the batch has spent so far (out[0..n-1], n <= 5): admissions, planning, CUDA
+   graph capture and instantiation, retirements, tuning (pm_batch_set_autotune). */
 int pm_batch_host_seconds(pm_batch* b, double* out, int n);
 
 #ifdef __cplusplus

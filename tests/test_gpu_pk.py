@@ -51,7 +51,13 @@ def run_pk_case(torch, n_parts, n_cells, box, steps, seed=0):
     from pmgpu.batch import Batch
     from pmgpu.config import Config, step_count
     cfg = Config(n_parts=n_parts, n_cells=n_cells, box_size=box, random_seed=seed, steps=steps)
-    pos, vel = ics.initial_conditions(cfg)
+    if n_parts > 256:  # the initial conditions on the device (the host restatement takes minutes)
+        from pmgpu.device_ics import DeviceICs
+        g = DeviceICs(n_parts)
+        pos, vel = g.generate(cfg)
+        g.close()
+    else:
+        pos, vel = ics.initial_conditions(cfg)
     nsteps = step_count(cfg.a_init, cfg.a_end, cfg.steps)
     b = Batch()
     sid = b.add(cfg, pos, vel)
@@ -102,6 +108,18 @@ def test_pk_after_full_run_256p_512g(cuda):
     res = run_pk_case(cuda, 256, 512, 250.0, 1000)
     record(res)
     print("P(k) 256^3/512^3:", {k: v for k, v in res.items() if not isinstance(v, list)})
+    assert res["pk_max_rel_dev"] < PK_TOL
+    assert res["mass_rel_err"] < 1e-6
+
+
+@pytest.mark.slow
+@pytest.mark.skipif(not os.environ.get("PM_FULL_RUNS"),
+                    reason="500 float64 oracle steps at 1024^3 take minutes: set PM_FULL_RUNS=1")
+def test_pk_after_full_run_512p_1024g(cuda):
+    """The large configuration: 512^3 particles, 1024^3 grid, box 500 Mpc/h, seed 1, 500 steps."""
+    res = run_pk_case(cuda, 512, 1024, 500.0, 500, seed=1)
+    record(res)
+    print("P(k) 512^3/1024^3:", {k: v for k, v in res.items() if not isinstance(v, list)})
     assert res["pk_max_rel_dev"] < PK_TOL
     assert res["mass_rel_err"] < 1e-6
 
