@@ -286,6 +286,9 @@ def run_gpu(args, ws, rank, local):
                 "frac": round(achieved / peak, 4), "peak_source": peak_src,
                 "traffic": traffic, "algorithmic_bytes": alg[dom], "launch_ms": round(prof[dom], 4),
                 "phase_ms": {k: round(v, 4) for k, v in prof.items()},
+                # every phase with algorithmic bytes: achieved / measured peak
+                "phase_frac": {k: round(alg[k] / (prof[k] / 1e3) / 1e9 / peak, 4) for k in prof
+                               if alg.get(k, 0) > 0 and prof[k] > 0},
                 "step_ms_sum_of_phases": round(sum(prof.values()), 4)}
 
     cpu = None
