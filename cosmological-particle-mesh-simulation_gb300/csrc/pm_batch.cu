@@ -131,6 +131,7 @@ struct pm_batch {
   std::map<int, std::vector<std::pair<DBuf, DBuf>>> grid_pool;
   std::map<long long, std::vector<std::pair<DBuf, DBuf>>> fin_pool;
   DBuf stage_pos, stage_vel;  // admission staging of host initial conditions
+  DBuf adm_count, adm_start, adm_cursor, adm_sums;  // row counting sort of an admission
   // pinned host staging of the plan's uploads (two, used in turn; an event marks when the
   // device has read one), so that re-planning never waits for enqueued work
   void* plan_host[2] = {nullptr, nullptr};
@@ -849,6 +850,10 @@ void pm_batch_destroy(pm_batch* b) {
     for (auto& g : e.second) { g.first.release(); g.second.release(); }
   b->stage_pos.release();
   b->stage_vel.release();
+  b->adm_count.release();
+  b->adm_start.release();
+  b->adm_cursor.release();
+  b->adm_sums.release();
   for (auto& t : b->tables) t.second->release();
   for (auto& l : b->lattices) l.second->release();
   b->sort.release();
@@ -949,9 +954,24 @@ int pm_batch_add(pm_batch* b, const pm_config* cfg, const float* positions, cons
     dp = b->stage_pos.as<float>();
     dv = b->stage_vel.as<float>();
   }
-  PB_CK(launch_abs_to_disp(dp, dv, r->np, r->np1, r->n, l->qi.as<int>(), l->qf.as<float>(), state(b, b->cur), off,
-                           st),
-        "convert");
+  {  // the state is written in row order (the counting sort of the new particles' rows), so that
+     // its first step reads it almost in order like every later one (a step sorts the state
+     // it writes)
+    const unsigned nrows = (unsigned)((long long)r->n * r->n);
+    PB_CK(b->adm_count.ensure_geo(sizeof(unsigned) * nrows), "alloc rows");
+    PB_CK(b->adm_start.ensure_geo(sizeof(unsigned) * ((size_t)nrows + 1)), "alloc rows");
+    PB_CK(b->adm_cursor.ensure_geo(sizeof(unsigned) * nrows), "alloc rows");
+    PB_CK(b->adm_sums.ensure_geo(sizeof(unsigned) * row_sort_block_sums(nrows)), "alloc rows");
+    unsigned* keys = b->sort.keys.as<unsigned>();  // free: the enqueued steps are done
+    unsigned* order = b->sort.vals.as<unsigned>();
+    PB_CK(launch_row_keys_abs(dp, r->np, r->n, keys, st), "admission keys");
+    PB_CK(row_counting_sort(keys, r->np, nrows, b->adm_count.as<unsigned>(), b->adm_start.as<unsigned>(),
+                            b->adm_cursor.as<unsigned>(), b->adm_sums.as<unsigned>(), order, nullptr, b->sms, st),
+          "admission sort");
+    PB_CK(launch_abs_to_disp(dp, dv, r->np, r->np1, r->n, l->qi.as<int>(), l->qf.as<float>(), state(b, b->cur),
+                             off, st, order),
+          "convert");
+  }
   PB_CK(cudaStreamSynchronize(st), "sync");
   r->in_off = off;
   b->in_total = off + r->np;

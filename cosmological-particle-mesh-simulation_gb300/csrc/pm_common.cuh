@@ -215,7 +215,9 @@ cudaError_t launch_tile_order(const Sim* sims, const Work& w, const unsigned* ro
                               unsigned* counts, int sms, cudaStream_t st);
 cudaError_t launch_abs_to_disp(const float* pos, const float* vel, long long np, int np1, int n,
                                const int* q_int, const float* q_frac, Parts out, long long off,
-                               cudaStream_t st);
+                               cudaStream_t st, const unsigned* order = nullptr);
+// keys[i] = x-row (tile order) of the cell of absolute position i (n^2 rows)
+cudaError_t launch_row_keys_abs(const float* pos, long long np, int n, unsigned* keys, cudaStream_t st);
 cudaError_t launch_disp_to_abs(Parts in, long long off, long long np, int np1, int n, const int* q_int,
                                const float* q_frac, float* pos, float* vel, cudaStream_t st);
 size_t deposit_smem_bytes(int n, int ty, int tz);

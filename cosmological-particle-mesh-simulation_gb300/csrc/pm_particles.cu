@@ -336,12 +336,23 @@ __global__ void k_coef(Sim* sims, int nsims, int advance) {
 // resident-state conversion: absolute (3, np) arrays in particle order <-> displacement
 // state at slots [off, off + np)
 // ---------------------------------------------------------------------------------
-__global__ void k_abs_to_disp(const float* __restrict__ pos, const float* __restrict__ vel, long long np,
-                              int np1, int n, const int* __restrict__ q_int, const float* __restrict__ q_frac,
-                              Parts out, long long off) {
-  const float fn = (float)n, half = 0.5f * fn;
+// x-row of the cell of every absolute position (the row part of the cell key, tile order)
+__global__ void k_row_keys_abs(const float* __restrict__ pos, long long np, int n, unsigned* __restrict__ keys) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < np;
        i += (long long)gridDim.x * blockDim.x) {
+    const Cell c = cell_abs(pos[i], pos[np + i], pos[2 * np + i], n);
+    keys[i] = c.ok ? row_number(c.y, c.z, n) : 0u;
+  }
+}
+
+// order (optional): slot off + i takes particle order[i] (the state is written in row order)
+__global__ void k_abs_to_disp(const float* __restrict__ pos, const float* __restrict__ vel, long long np,
+                              int np1, int n, const int* __restrict__ q_int, const float* __restrict__ q_frac,
+                              Parts out, long long off, const unsigned* __restrict__ order) {
+  const float fn = (float)n, half = 0.5f * fn;
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < np;
+       s += (long long)gridDim.x * blockDim.x) {
+    const long long i = order ? (long long)__ldg(&order[s]) : s;  // the particle
     const unsigned id = (unsigned)i, u1 = (unsigned)np1;
     const unsigned ax[3] = {id / (u1 * u1), (id / u1) % u1, id % u1};
     float* dst[3] = {out.x, out.y, out.z};
@@ -352,10 +363,10 @@ __global__ void k_abs_to_disp(const float* __restrict__ pos, const float* __rest
       float d = pos[k * np + i] - q;
       if (d >= half) d -= fn;
       if (d < -half) d += fn;
-      dst[k][off + i] = d;
-      vdst[k][off + i] = vel[k * np + i];
+      dst[k][off + s] = d;
+      vdst[k][off + s] = vel[k * np + i];
     }
-    out.id[off + i] = pack_lattice(ax[0], ax[1], ax[2]);
+    out.id[off + s] = pack_lattice(ax[0], ax[1], ax[2]);
   }
 }
 
@@ -388,10 +399,17 @@ __global__ void k_disp_to_abs(Parts in, long long off, long long np, int np1, in
 // ---------------------------------------------------------------------------------
 cudaError_t launch_abs_to_disp(const float* pos, const float* vel, long long np, int np1, int n,
                                const int* q_int, const float* q_frac, Parts out, long long off,
-                               cudaStream_t st) {
+                               cudaStream_t st, const unsigned* order) {
   long long b = (np + 255) / 256;
   if (b > 152 * 32) b = 152 * 32;
-  k_abs_to_disp<<<(int)b, 256, 0, st>>>(pos, vel, np, np1, n, q_int, q_frac, out, off);
+  k_abs_to_disp<<<(int)b, 256, 0, st>>>(pos, vel, np, np1, n, q_int, q_frac, out, off, order);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_row_keys_abs(const float* pos, long long np, int n, unsigned* keys, cudaStream_t st) {
+  long long b = (np + 255) / 256;
+  if (b > 152 * 32) b = 152 * 32;
+  k_row_keys_abs<<<(int)(b > 0 ? b : 1), 256, 0, st>>>(pos, np, n, keys);
   return cudaGetLastError();
 }
 
