@@ -136,13 +136,13 @@ __device__ __forceinline__ unsigned source_slot(const unsigned* __restrict__ per
 }
 
 // Base cell of a source particle relative to the tile, from its loaded words; false if
-// absent or bad.
-template <int MODE>
+// absent or bad.  NN: the grid size when known at compile time (0: S.n).
+template <int MODE, int NN>
 __device__ __forceinline__ bool source_cell(const Sim& S, const Parts& p, const RawCell& raw, int y0, int z0,
                                             int* err, Cell& c, int& ly, int& lz) {
   if (!raw.present) return false;
   c = raw_cell<MODE>(S, p, raw);
-  const int n = S.n;
+  const int n = NN ? NN : S.n;
   int dy = c.y - y0, dz = c.z - z0;
   if (dy >= n - 1) dy -= n;
   if (dz >= n - 1) dz -= n;
@@ -205,13 +205,13 @@ __device__ __forceinline__ void run_table(const RunLoad& v, int lane, unsigned* 
 // The particle loop of a tile: two source entries per lane and iteration, so that their
 // loads overlap; the slots (the permutation entries) of the next iteration are in flight
 // while this one adds its particles.
-template <int MODE, int NT, bool ONE>
+template <int MODE, int NT, bool ONE, int NN>
 __device__ __forceinline__ void deposit_sources(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
                                                 int* err, int y0, int z0, unsigned* lo, unsigned* hi, int rs,
                                                 const unsigned* s_begin, const unsigned* s_off, unsigned total,
                                                 float qscale, int tid) {
   const int lane = tid & 31, warp = tid >> 5;
-  const int n = S.n;
+  const int n = NN ? NN : S.n;
   unsigned base = (unsigned)warp * 32u;
   unsigned sl0 = source_slot(perm, s_begin, s_off, base + lane, total);
   unsigned sl1 = source_slot(perm, s_begin, s_off, base + NT + lane, total);
@@ -221,8 +221,8 @@ __device__ __forceinline__ void deposit_sources(const Sim& S, const Parts& p, co
     sl1 = source_slot(perm, s_begin, s_off, base + 3 * NT + lane, total);
     Cell c0, c1;
     int ly0 = 0, lz0 = 0, ly1 = 0, lz1 = 0;
-    const bool ok0 = source_cell<MODE>(S, p, q0, y0, z0, err, c0, ly0, lz0);
-    const bool ok1 = source_cell<MODE>(S, p, q1, y0, z0, err, c1, ly1, lz1);
+    const bool ok0 = source_cell<MODE, NN>(S, p, q0, y0, z0, err, c0, ly0, lz0);
+    const bool ok1 = source_cell<MODE, NN>(S, p, q1, y0, z0, err, c1, ly1, lz1);
     deposit_entry<ONE>(lo, hi, n, rs, qscale, ok0, c0, ly0, lz0);
     deposit_entry<ONE>(lo, hi, n, rs, qscale, ok1, c1, ly1, lz1);
   }
@@ -233,8 +233,9 @@ __device__ __forceinline__ void deposit_sources(const Sim& S, const Parts& p, co
 // tiles).  s_begin / s_off: NRUN + 1 words each, already holding the tile's run table when
 // runs_ready.  Done by NT threads, tid = 0 .. NT - 1 (a whole CTA, or a group of its warps
 // with one tile each: every group calls it together, it synchronises the whole CTA).  Returns
-// how the sums are held (tile_sum), also written to *ts_out when given.
-template <int MODE, int NT>
+// how the sums are held (tile_sum), also written to *ts_out when given.  NN: the grid size
+// when known at compile time (0: S.n).
+template <int MODE, int NT, int NN = 0>
 __device__ __forceinline__ TileSum deposit_tile(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
                                                 const unsigned* __restrict__ row_start, int* err, int y0, int z0,
                                                 unsigned* lo, unsigned* hi, int rs, unsigned* s_begin,
@@ -242,7 +243,7 @@ __device__ __forceinline__ TileSum deposit_tile(const Sim& S, const Parts& p, co
                                                 TileSum* ts_out = nullptr) {
   if (tid < 0) tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
-  const int n = S.n;
+  const int n = NN ? NN : S.n;
   if (!runs_ready) {
     if (warp == 0) run_table(run_load(S, row_start, y0, z0, lane), lane, s_begin, s_off, lane < 8);
     __syncthreads();
@@ -259,10 +260,10 @@ __device__ __forceinline__ TileSum deposit_tile(const Sim& S, const Parts& p, co
   }
   __syncthreads();
   if (ts.s)
-    deposit_sources<MODE, NT, true>(S, p, perm, err, y0, z0, lo, hi, rs, s_begin, s_off, total,
+    deposit_sources<MODE, NT, true, NN>(S, p, perm, err, y0, z0, lo, hi, rs, s_begin, s_off, total,
                                     __uint_as_float((unsigned)(127 + ts.s) << 23), tid);
   else
-    deposit_sources<MODE, NT, false>(S, p, perm, err, y0, z0, lo, hi, rs, s_begin, s_off, total,
+    deposit_sources<MODE, NT, false, NN>(S, p, perm, err, y0, z0, lo, hi, rs, s_begin, s_off, total,
                                      (float)(1u << PM_FIX_BITS), tid);
   __syncthreads();
   return ts;

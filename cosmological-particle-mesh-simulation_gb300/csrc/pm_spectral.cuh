@@ -845,7 +845,7 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
       {  // the particles of this group's tile (a group without a tile has an empty table)
         int si, y0, z0;
         tile_of(idx + g, si, y0, z0);
-        deposit_tile<MODE, NTT>(sims[si], p, perm, row_start, err, y0, z0, lo + g * NL * RS, hi + g * NL * RS, RS,
+        deposit_tile<MODE, NTT, N>(sims[si], p, perm, row_start, err, y0, z0, lo + g * NL * RS, hi + g * NL * RS, RS,
                                 s_begin[g], s_off[g], true, gtid, &s_ts[g]);
       }
       // the CTA's TPB * NL rows: T lanes per row, rows R = warp * RPW + sub; a row's exchange
@@ -898,7 +898,7 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
       int si, y0, z0;
       tile_of(idx, si, y0, z0);
       const Sim& S = sims[si];
-      const TileSum ts = deposit_tile<MODE, NT>(S, p, perm, row_start, err, y0, z0, lo, hi, RS, s_begin[0], s_off[0],
+      const TileSum ts = deposit_tile<MODE, NT, N>(S, p, perm, row_start, err, y0, z0, lo, hi, RS, s_begin[0], s_off[0],
                                                 runs_ready);
       runs_ready = false;
       float v[PER];
