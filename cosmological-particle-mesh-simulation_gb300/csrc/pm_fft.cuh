@@ -277,19 +277,21 @@ __device__ __forceinline__ void fft_passes(float2* s, const float2* __restrict__
   }
 }
 
-// Lengths whose blocked transforms run on pairs of lines (the radix-3 plans hold too many
-// values per thread for it).
-__host__ __device__ constexpr bool blocked_pairs(int L) { return L % 3 != 0; }
+// Lengths whose blocked transforms run on pairs of lines: all but the radix-3 plans other
+// than 192 and 384, whose tasks per pair overflow the registers (96 and 768 spill; 192 and
+// 384 on pairs measured 0.58 -> 0.50 and 0.91 -> 0.79 ms per 134M-cell z pass).
+__host__ __device__ constexpr bool blocked_pairs(int L) { return L % 3 != 0 || L == 192 || L == 384; }
 
 // Whether task j of a stride-1 pass over NP pairs of lines stores its R outputs in the order
 // r ^ 1: with 4 pairs, the 8 lanes of a quarter-warp (one phase of a 128-bit shared-memory
 // access) hold j and j + 1, whose outputs R j + r lie R 16-byte words apart -- a multiple
 // of the 8 words of a bank row, so in the same banks.  Odd j then write the neighbouring
 // word first, which sits 4 banks over: conflict-free phases.  The swap costs selects, so
-// only the shared-memory-bound z pass takes it (BANKS); the HBM-bound y passes do not.
-template <int NS, int NP>
+// only the shared-memory-bound z pass takes it (BANKS); the HBM-bound y passes do not.  The
+// swap pairs outputs r and r ^ 1, so the radix R must be even.
+template <int NS, int NP, int R>
 __device__ __forceinline__ bool store_swap(int j) {
-  return NS == 1 && NP == 4 && (j & 1);
+  return NS == 1 && NP == 4 && R % 2 == 0 && (j & 1);
 }
 
 // The same pass over pairs of adjacent lines of the Blocked layout (BW even): the two lines
@@ -339,7 +341,7 @@ __device__ __forceinline__ void stockham_pass_pairs(float2* s, const float2* __r
       const int base = (j - k) * R + k;
       // stride-1 stores of 4 pairs per j: the 8 lanes of a quarter-warp hold two j whose
       // outputs fall in the same banks; odd j store in the order r ^ 1 (other banks)
-      const bool sw = BANKS && store_swap<NS, NP>(j);
+      const bool sw = BANKS && store_swap<NS, NP, R>(j);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int e = base + (sw ? r ^ 1 : r) * NS;
@@ -447,7 +449,7 @@ __device__ __forceinline__ void stockham_turn(float2* s, const float2* __restric
       // inverse, first pass (stride 1: no twiddles), outputs j R + r
       DFT<R, true>::run(a[t]);
       if constexpr (PAIRS) DFT<R, true>::run(b[t]);
-      const bool sw = PAIRS && store_swap<1, NG>(j);
+      const bool sw = PAIRS && store_swap<1, NG, R>(j);
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int rr = sw ? r ^ 1 : r;

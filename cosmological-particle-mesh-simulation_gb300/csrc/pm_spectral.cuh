@@ -30,9 +30,10 @@ __host__ __device__ constexpr int cx_rows(int n) {
   // rows of the x passes per CTA: ~SP_ELEMS complex, a multiple of 8, at most n*n
   return (SP_ELEMS / (n / 2)) / 8 * 8 > n * n ? n * n : (SP_ELEMS / (n / 2)) / 8 * 8;
 }
-// Line passes of the 512 grid run two CTAs per SM, each with 32 KB TMA
-// stages of bundles 8 columns wide; the others one CTA with 64 KB stages.
-__host__ __device__ constexpr bool line_small(int n) { return n == 512; }
+// Line passes of the 512 and 384 grids run two CTAs per SM, each with 32 / 24 KB TMA
+// stages of bundles 8 columns wide; the others one CTA with 64 KB stages (measured: 8-wide
+// bundles slow the 256 grid's z pass 0.34 -> 0.41 ms and the 192 grid's 0.50 -> 0.52 ms).
+__host__ __device__ constexpr bool line_small(int n) { return n == 512 || n == 384; }
 // columns of a line-pass bundle
 __host__ __device__ constexpr int cline_width(int n) { return n >= 512 || line_small(n) ? 8 : 16; }
 // bundles per unit (per TMA stage)
@@ -49,11 +50,9 @@ __host__ __device__ constexpr int cpitch(int n) { return (chalf(n) + 15) / 16 * 
 // Line passes that stream through a TMA ring: boxes of at most 256 rows tiling n.
 __host__ __device__ constexpr int line_box_rows(int n) { return n <= 256 ? n : (n % 256 == 0 ? 256 : n / 2); }
 __host__ __device__ constexpr bool tma_lines(int n) { return n >= 32 && line_box_rows(n) <= 256; }
-// Threads of a line-pass CTA: 512 (pairs of lines, up to 128 registers), 256 for the
-// two-CTA sizes; the radix-3 sizes from 192 up, transformed line by line, run 1024.
-__host__ __device__ constexpr int line_nt(int n) {
-  return line_small(n) ? 256 : (n % 3 == 0 && n >= 192 ? 1024 : 512);
-}
+// Threads of a line-pass CTA: 512 (up to 128 registers), 256 for the two-CTA sizes; 768,
+// transformed line by line, runs 1024.
+__host__ __device__ constexpr int line_nt(int n) { return line_small(n) ? 256 : (n == 768 ? 1024 : 512); }
 __host__ __device__ constexpr int line_ctas_per_sm(int n) { return line_small(n) ? 2 : 1; }
 constexpr int XTMA_NT = 1024;  // x passes
 constexpr int TMA_STAGES = 3;
@@ -770,15 +769,18 @@ __host__ __device__ constexpr bool deposit_r2c_ok(int n) { return (TZ * TY * n) 
 // Tiles per CTA of the fused deposit: the register row transform of a tile's 16 rows keeps
 // 16 / T warps busy (T lanes per row), so on the sizes with T < 16 a CTA takes several tiles
 // at once -- its warps split into one group per tile for the particle loop and share all the
-// rows in the transform -- as long as their accumulators stay within 72 KB (three CTAs per SM).
+// rows in the transform -- as long as their accumulators stay within 72 KB (three CTAs per
+// SM).  The 192 grid (T = 4, 48 complex values per lane) takes its four tiles at two CTAs per
+// SM with 128 registers instead (measured 0.90 -> 0.87 ms per 134M-cell deposit).
+__host__ __device__ constexpr int dep_ctas_bound(int n) { return n == 192 ? 2 : (xrow_ok(n) ? 3 : 2); }
 __host__ __device__ constexpr int dep_tiles(int n) {
   int t = xrow_ok(n) ? 16 / xrow_T(n) : 1;
-  while (t > 1 && (size_t)t * deposit_r2c_smem_bytes(n) > 72 * 1024) t /= 2;
+  while (t > 1 && (size_t)t * deposit_r2c_smem_bytes(n) > (n == 192 ? 100 : 72) * 1024) t /= 2;
   return t;
 }
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(deposit_r2c_nt(N), xrow_ok(N) ? 3 : 2)
+__global__ void __launch_bounds__(deposit_r2c_nt(N), dep_ctas_bound(N))
     k_deposit_r2c(const Sim* __restrict__ sims, Work w, Parts p, const unsigned* __restrict__ perm,
                   const unsigned* __restrict__ row_start, int* err, unsigned* __restrict__ next_tile,
                   const unsigned* __restrict__ order) {
