@@ -410,8 +410,16 @@ def measure_batched(args, local):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / 1e3
 
-    b = Batch(device=local)
-    ids = [b.add(c, p, v) for c, (p, v) in zip(cfgs, ics_)]
+    def wall(fn):  # host seconds of set-up work, the device idle on both sides
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t
+
+    b, setup_batch = wall(lambda: Batch(device=local))
+    ids, t_add = wall(lambda: [b.add(c, p, v) for c, (p, v) in zip(cfgs, ics_)])
+    setup_batch += t_add
     t_batch = timed(lambda: b.step(max(steps) + 1))
     b.check_device()
     assert all(b.state(i)[1] == k for i, k in zip(ids, steps))
@@ -424,16 +432,25 @@ def measure_batched(args, local):
     launches = pb.launches_per_step()
     pb.close()
 
-    def plain():
-        for c, (p, v) in zip(cfgs, ics_):
-            one = Batch(device=local)
-            one.add(c, p, v)
-            one.step(step_count(c.a_init, c.a_end, c.steps) + 1)
-            one.close()
-    t_plain = timed(plain)
+    # each simulation alone: its set-up (batch, admission) on the host clock, its steps on the
+    # device clock, like the batched run's
+    t_plain, setup_plain, by_size = 0.0, 0.0, {}
+    for c, (p, v) in zip(cfgs, ics_):
+        one, t_new = wall(lambda: Batch(device=local))
+        _, t_one_add = wall(lambda: one.add(c, p, v))
+        t_one = timed(lambda: one.step(step_count(c.a_init, c.a_end, c.steps) + 1))
+        one.close()
+        t_plain += t_one
+        setup_plain += t_new + t_one_add
+        by_size[c.n_cells] = by_size.get(c.n_cells, 0.0) + t_one
     return {"value": pu / t_batch, "unit": UNIT, "plain_value": pu / t_plain,
-            "batched_over_plain": t_plain / t_batch, "sims": len(cfgs), "particle_updates": pu,
-            "seconds_batched": round(t_batch, 3), "seconds_plain": round(t_plain, 3), "ics_seconds": round(t_ics, 2),
+            "batched_over_plain": t_plain / t_batch,
+            "batched_over_plain_with_setup": (t_plain + setup_plain) / (t_batch + setup_batch),
+            "sims": len(cfgs), "particle_updates": pu,
+            "seconds_batched": round(t_batch, 3), "seconds_plain": round(t_plain, 3),
+            "setup_seconds_batched": round(setup_batch, 3), "setup_seconds_plain": round(setup_plain, 3),
+            "seconds_plain_by_grid": {k: round(v, 3) for k, v in sorted(by_size.items())},
+            "ics_seconds": round(t_ics, 2),
             "batched_phase_ms": {k: round(v, 4) for k, v in prof.items()}, "launches_per_step": launches,
             "schedule": schedule,
             "workload": f"{len(cfgs)} simulations, seeds 0-{len(cfgs) - 1}, N_PARTS in {{32,48,64,96,128}}, "

@@ -110,8 +110,8 @@ struct pm_batch {
   int cur = 0;
   SortBufs sort;
   DBuf row_start, d_sims, d_prefix, d_err, d_maps;
-  DBuf tile_next;   // tile counter of the fused deposit, and 2 words of scratch for the ordering
-  DBuf tile_order;  // the fused deposit's tiles, dense first
+  DBuf tile_next;   // per distinct size: tile counter of the fused deposit, 2 words of ordering scratch
+  DBuf tile_order;  // per distinct size (at its tile prefix): the fused deposit's tiles, dense first
   DBuf d_one;       // descriptor + work table of a one-simulation deposit (pm_batch_density)
   DBuf row_count, row_cursor, scan_sums;  // counting sort of the row keys
   Plan plan;
@@ -126,6 +126,12 @@ struct pm_batch {
   cudaStream_t own = nullptr;     // used when the caller passes the legacy stream (captures need one)
   cudaStream_t admit = nullptr;   // admission conversions
   cudaEvent_t last_step = nullptr;  // recorded after the last enqueued step
+  // The spectral chains of the distinct grid sizes (fused deposit, y, z, y^-1, x C2R) touch
+  // disjoint grids: a step runs them on one stream per size, forked after the sort and joined
+  // before the kick, so that the kernels of one size fill the tails of another's.
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> side_ev;
+  cudaEvent_t fork_ev = nullptr;
   // grids (potential, spectrum) of retired simulations by grid size, and final-state
   // buffers by particle count, kept for reuse
   std::map<int, std::vector<std::pair<DBuf, DBuf>>> grid_pool;
@@ -138,7 +144,9 @@ struct pm_batch {
   size_t plan_host_bytes[2] = {0, 0};
   cudaEvent_t plan_ev[2] = {nullptr, nullptr};
   int plan_turn = 0;
-  double host_s[5] = {0, 0, 0, 0, 0};  // host seconds: admission, planning, graph capture, retirement, tuning
+  // host seconds: admission, planning, graph capture, retirement, tuning, and the part of
+  // planning spent waiting for the device to release a staging buffer (not in planning's)
+  double host_s[6] = {0, 0, 0, 0, 0, 0};
   std::string err;
 };
 
@@ -392,8 +400,20 @@ int build_plan(pm_batch* b, cudaStream_t st) {
   PB_CK(b->row_count.ensure_geo(sizeof(unsigned) * (size_t)rows), "alloc rows");
   {
     size_t tiles = 1;
-    for (int t : P.fdep_total) tiles = std::max(tiles, (size_t)t);
+    for (int t : P.fdep_total) tiles += (size_t)t;
     PB_CK(b->tile_order.ensure_geo(sizeof(unsigned) * tiles), "alloc tile order");
+    PB_CK(b->tile_next.ensure_geo(4 * sizeof(unsigned) * P.sizes.size()), "alloc tile counters");
+    while (b->side.size() < P.sizes.size()) {
+      cudaStream_t s = nullptr;
+      cudaEvent_t e = nullptr;
+      PB_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+      if (cudaError_t ee = cudaEventCreateWithFlags(&e, cudaEventDisableTiming)) {
+        cudaStreamDestroy(s);
+        return bcuda(b, ee, "event");
+      }
+      b->side.push_back(s);
+      b->side_ev.push_back(e);
+    }
   }
   PB_CK(b->row_cursor.ensure_geo(sizeof(unsigned) * (size_t)rows), "alloc rows");
   PB_CK(b->scan_sums.ensure_geo(sizeof(unsigned) * row_sort_block_sums(rows)), "alloc rows");
@@ -402,7 +422,15 @@ int build_plan(pm_batch* b, cudaStream_t st) {
     const size_t o_sims = (mb + 255) / 256 * 256, o_pre = o_sims + (sbytes + 255) / 256 * 256, total = o_pre + pbytes;
     const int t = b->plan_turn;
     if (!b->plan_ev[t]) PB_CK(cudaEventCreateWithFlags(&b->plan_ev[t], cudaEventDisableTiming), "event");
-    else PB_CK(cudaEventSynchronize(b->plan_ev[t]), "staging");  // its last uploads have been read
+    else {  // its last uploads have been read
+      double waited = 0;
+      {
+        HostTimer wt(waited);
+        PB_CK(cudaEventSynchronize(b->plan_ev[t]), "staging");
+      }
+      b->host_s[1] -= waited;  // (the planning timer adds the whole scope)
+      b->host_s[5] += waited;
+    }
     if (b->plan_host_bytes[t] < total) {
       if (b->plan_host[t]) cudaFreeHost(b->plan_host[t]);
       b->plan_host[t] = nullptr;
@@ -473,6 +501,10 @@ int enqueue_deposit(pm_batch* b, int g, const Shape& sh, Parts in, const unsigne
   int* err = b->d_err.as<int>();
   const int n = P.sizes[g], tot = P.fdep_total[g];
   const Work wg = work_of(b, PH_FIXED + 3 * g + 2, tot);
+  // this size's tile counter and ordering scratch, and its part of the tile order
+  unsigned* next = b->tile_next.as<unsigned>() + 4 * g;
+  unsigned* order = b->tile_order.as<unsigned>();
+  for (int i = 0; i < g; ++i) order += P.fdep_total[i];
   if (sh.dep == DEP_SEPARATE) {
     PB_CK(launch_deposit(ds, wg, in, perm, b->row_start.as<unsigned>(), POS_DISP, err, grid_for(tot, b->sms, 3),
                          deposit_smem_bytes(n, TILE_Y, TILE_Z), st),
@@ -480,12 +512,9 @@ int enqueue_deposit(pm_batch* b, int g, const Shape& sh, Parts in, const unsigne
     return PM_OK;
   }
   if (sh.dep == DEP_FUSED_DENSE_FIRST)
-    PB_CK(launch_tile_order(ds, wg, b->row_start.as<unsigned>(), b->tile_order.as<unsigned>(),
-                            b->tile_next.as<unsigned>() + 2, b->sms, st),
-          "tile order");
-  PB_CK(deposit_r2c_dispatch(n, ds, wg, in, perm, b->row_start.as<unsigned>(), POS_DISP, err,
-                             b->tile_next.as<unsigned>(),
-                             sh.dep == DEP_FUSED_DENSE_FIRST ? b->tile_order.as<unsigned>() : nullptr,
+    PB_CK(launch_tile_order(ds, wg, b->row_start.as<unsigned>(), order, next + 2, b->sms, st), "tile order");
+  PB_CK(deposit_r2c_dispatch(n, ds, wg, in, perm, b->row_start.as<unsigned>(), POS_DISP, err, next,
+                             sh.dep == DEP_FUSED_DENSE_FIRST ? order : nullptr,
                              grid_for(tot, b->sms, sh.dep_cps ? sh.dep_cps : deposit_r2c_ctas_per_sm(n)), st),
         "fused deposit");
   return PM_OK;
@@ -513,24 +542,44 @@ int enqueue_step(pm_batch* b, int cur, cudaStream_t st, cudaEvent_t* ev = nullpt
     PB_CK(launch_deposit(ds, work_of(b, PH_DEP, P.fixed_total[PH_DEP]), in, perm, b->row_start.as<unsigned>(),
                          POS_DISP, err, grid_for(P.fixed_total[PH_DEP], b->sms, 3), P.max_dep_smem, st),
           "deposit");
-  for (size_t g = 0; g < P.sizes.size(); ++g)
-    if (P.fused[g])
-      if (int r = enqueue_deposit(b, (int)g, P.shape[g], in, perm, st)) return r;
-  PB_CK(mark(1 + PP_DEPOSIT), "event");
   const SpecKind order[5] = {SPEC_X_R2C, SPEC_Y_FWD, SPEC_Z_GREEN, SPEC_Y_INV, SPEC_X_C2R};
-  for (int o = 0; o < 5; ++o) {
+  auto spectral = [&](int o, int g, cudaStream_t s) -> int {
     const SpecKind k = order[o];
+    if (k == SPEC_X_R2C && P.shape[g].dep != DEP_SEPARATE) return PM_OK;  // done by the fused deposit
+    const bool xk = (k == SPEC_X_R2C || k == SPEC_X_C2R);
+    const int ph = PH_FIXED + 3 * g + (xk ? 0 : 1);
+    const int tot = xk ? P.x_total[g] : P.line_total[g];
+    PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot),
+                            xk ? grid_for(tot, b->sms, P.shape[g].x_cps) : grid_for(tot, b->sms, 8), s,
+                            b->d_maps.as<CUtensorMap>(), err),
+          "spectral");
+    return PM_OK;
+  };
+  if (!ev && P.sizes.size() > 1 && b->side.size() >= P.sizes.size()) {
+    // one stream per distinct size: deposit and transforms of that size in order, the sizes
+    // side by side
+    PB_CK(cudaEventRecord(b->fork_ev, st), "event");
     for (size_t g = 0; g < P.sizes.size(); ++g) {
-      if (k == SPEC_X_R2C && P.shape[g].dep != DEP_SEPARATE) continue;  // done by the fused deposit
-      const bool xk = (k == SPEC_X_R2C || k == SPEC_X_C2R);
-      const int ph = PH_FIXED + 3 * (int)g + (xk ? 0 : 1);
-      const int tot = xk ? P.x_total[g] : P.line_total[g];
-      PB_CK(spectral_dispatch(k, P.sizes[g], ds, work_of(b, ph, tot),
-                              xk ? grid_for(tot, b->sms, P.shape[g].x_cps) : grid_for(tot, b->sms, 8), st,
-                              b->d_maps.as<CUtensorMap>(), err),
-            "spectral");
+      cudaStream_t s = b->side[g];
+      PB_CK(cudaStreamWaitEvent(s, b->fork_ev, 0), "fork");
+      if (P.fused[g])
+        if (int r = enqueue_deposit(b, (int)g, P.shape[g], in, perm, s)) return r;
+      for (int o = 0; o < 5; ++o)
+        if (int r = spectral(o, (int)g, s)) return r;
+      PB_CK(cudaEventRecord(b->side_ev[g], s), "event");
+      PB_CK(cudaStreamWaitEvent(st, b->side_ev[g], 0), "join");
     }
-    PB_CK(mark(1 + PP_X_R2C + o), "event");
+  } else {
+    // phase by phase (the profiled order: an event after every phase)
+    for (size_t g = 0; g < P.sizes.size(); ++g)
+      if (P.fused[g])
+        if (int r = enqueue_deposit(b, (int)g, P.shape[g], in, perm, st)) return r;
+    PB_CK(mark(1 + PP_DEPOSIT), "event");
+    for (int o = 0; o < 5; ++o) {
+      for (size_t g = 0; g < P.sizes.size(); ++g)
+        if (int r = spectral(o, (int)g, st)) return r;
+      PB_CK(mark(1 + PP_X_R2C + o), "event");
+    }
   }
   // the kick writes the next keys and counts them per row for the next step's sort
   PB_CK(cudaMemsetAsync(b->row_count.p, 0, sizeof(unsigned) * (size_t)P.rows, st), "count reset");
@@ -823,6 +872,7 @@ int pm_batch_create(int device, size_t mem_cap_bytes, pm_batch** out) {
   if (!e) e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
   if (!e) e = cudaStreamCreateWithFlags(&b->admit, cudaStreamNonBlocking);
   if (!e) e = cudaEventCreateWithFlags(&b->last_step, cudaEventDisableTiming);
+  if (!e) e = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
   if (!e) e = cudaDeviceSynchronize();
   if (e) {
     pm_batch_destroy(b);
@@ -875,6 +925,9 @@ void pm_batch_destroy(pm_batch* b) {
     if (b->plan_host[t]) cudaFreeHost(b->plan_host[t]);
   }
   if (b->last_step) cudaEventDestroy(b->last_step);
+  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+  for (auto s : b->side) cudaStreamDestroy(s);
+  for (auto e : b->side_ev) cudaEventDestroy(e);
   delete b;
 }
 
@@ -1175,7 +1228,7 @@ int pm_batch_schedule(pm_batch* b, int* out, int cap) {
 
 int pm_batch_host_seconds(pm_batch* b, double* out, int n) {
   if (!b || !out || n < 0) return PM_ERR_ARG;
-  for (int i = 0; i < n && i < 5; ++i) out[i] = b->host_s[i];
+  for (int i = 0; i < n && i < 6; ++i) out[i] = b->host_s[i];
   return PM_OK;
 }
 

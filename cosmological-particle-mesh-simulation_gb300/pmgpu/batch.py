@@ -152,10 +152,12 @@ class Batch:
         return out
 
     def host_seconds(self) -> dict:
-        """Host time spent so far in admissions, planning, graph capture, retirements and tuning."""
-        arr = (ctypes.c_double * 5)()
-        self._check(self._lib.pm_batch_host_seconds(self._h, arr, 5))
-        return dict(zip(("admit", "plan", "capture", "retire", "tune"), [round(float(x), 4) for x in arr]))
+        """Host time spent so far in admissions, planning, graph capture, retirements and tuning,
+        and the time planning waited for enqueued steps (``plan_wait``, not in ``plan``)."""
+        arr = (ctypes.c_double * 6)()
+        self._check(self._lib.pm_batch_host_seconds(self._h, arr, 6))
+        return dict(zip(("admit", "plan", "capture", "retire", "tune", "plan_wait"),
+                        [round(float(x), 4) for x in arr]))
 
     def launches_per_step(self) -> int:
         return int(self._lib.pm_batch_launches_per_step(self._h))

@@ -222,8 +222,10 @@ int pm_batch_set_autotune(pm_batch* b, int enable);
    1 fused index order / 2 separate, fused-deposit CTAs per SM, x-pass CTAs per SM), then
    (0, kick CTAs per SM, 1 if tuned, 0).  Returns the ints written (-1 on error). */
 int pm_batch_schedule(pm_batch* b, int* out, int cap);
-/* Host seconds the batch has spent so far (out[0..n-1], n <= 5): admissions, planning, CUDA
-   graph capture and instantiation, retirements, tuning (pm_batch_set_autotune). */
+/* Host seconds the batch has spent so far (out[0..n-1], n <= 6): admissions, planning, CUDA
+   graph capture and instantiation, retirements, tuning (pm_batch_set_autotune), and the time
+   planning waited for the device to finish reading an earlier plan's uploads (back-pressure
+   from enqueued steps; not counted in planning). */
 int pm_batch_host_seconds(pm_batch* b, double* out, int n);
 
 #ifdef __cplusplus
