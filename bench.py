@@ -126,6 +126,36 @@ def job_throughput(particles, steps, ranks, seconds):
     return particles * steps * ranks / seconds
 
 
+def host_link(local, nbytes, reps=5):
+    """Host-link bandwidth between pinned host memory and this GPU (GB/s): one direction at a
+    time, and both at once on two streams (the copies the e2e step makes each step)."""
+    import torch
+    n = nbytes // 4
+    h_in = torch.empty(n, dtype=torch.float32).pin_memory()
+    h_out = torch.empty(n, dtype=torch.float32).pin_memory()
+    d_a = torch.empty(n, dtype=torch.float32, device=f"cuda:{local}")
+    d_b = torch.empty(n, dtype=torch.float32, device=f"cuda:{local}")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def run(h2d, d2h):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            if h2d:
+                with torch.cuda.stream(s1):
+                    d_a.copy_(h_in, non_blocking=True)
+            if d2h:
+                with torch.cuda.stream(s2):
+                    h_out.copy_(d_b, non_blocking=True)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps
+
+    run(True, True)  # warm-up
+    t_in, t_out, t_both = run(True, False), run(False, True), run(True, True)
+    return {"h2d": round(nbytes / t_in / 1e9, 1), "d2h": round(nbytes / t_out / 1e9, 1),
+            "both_each_way": round(nbytes / t_both / 1e9, 1), "bytes": nbytes}
+
+
 def measured_peak():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -270,6 +300,12 @@ def run_gpu(args, ws, rank, local):
                "h2d_bytes_per_step": 2 * 3 * 4 * np_, "d2h_bytes_per_step": 2 * 3 * 4 * np_,
                "steps": args.e2e_steps, "api": "pm_step_host (C ABI, pinned host arrays)"}
         ctx.close()
+        # the host link the step's copies cross: its floor is the step's bytes each way at the
+        # bandwidth both directions reach together
+        link = host_link(local, 2 * 3 * 4 * np_)
+        e2e["host_link_gbs"] = link
+        e2e["link_floor_ms"] = round(2 * 3 * 4 * np_ / (link["both_each_way"] * 1e9) * 1e3, 3)
+        e2e["ms_per_step"] = round(te / args.e2e_steps * 1e3, 3)
 
     if rank != 0:
         if dist is not None:

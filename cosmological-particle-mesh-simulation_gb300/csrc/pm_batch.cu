@@ -122,7 +122,12 @@ struct pm_batch {
   int plan_steps = 0;       // steps run since the plan was built
   bool sparse = false;      // the state the next step reads has empty slots (after a retirement)
   long long in_total = 0;   // slots of that state
+  // Executable graphs of a step from state 0 and from state 1.  A new plan marks them stale:
+  // the next capture updates them in place (cudaGraphExecUpdate, no instantiation) and only
+  // a change of the graph's shape instantiates a new one -- destroying an executable graph
+  // synchronises with the device, which stalled the serving loop at every re-plan.
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  bool gstale[2] = {false, false};
   cudaStream_t own = nullptr;     // used when the caller passes the legacy stream (captures need one)
   cudaStream_t admit = nullptr;   // admission conversions
   cudaEvent_t last_step = nullptr;  // recorded after the last enqueued step
@@ -272,11 +277,24 @@ cudaError_t grow_state(pm_batch* b, long long need) {
   return b->sort.ensure(cap);
 }
 
-void drop_graphs(pm_batch* b) {
-  for (auto& g : b->gexec) {
-    if (g) cudaGraphExecDestroy(g);
-    g = nullptr;
+// The step graphs no longer match the plan: marked stale (updated at their next capture), or
+// destroyed with `destroy`.  Returns the host seconds it took (counted as graph work:
+// capture, instantiation, update and destruction).
+double drop_graphs(pm_batch* b, bool destroy = false) {
+  double s = 0;
+  {
+    HostTimer timer(s);
+    for (int c = 0; c < 2; ++c) {
+      b->gstale[c] = b->gexec[c] != nullptr;
+      if (destroy && b->gexec[c]) {
+        cudaGraphExecDestroy(b->gexec[c]);
+        b->gexec[c] = nullptr;
+        b->gstale[c] = false;
+      }
+    }
   }
+  b->host_s[2] += s;
+  return s;
 }
 
 Tables* tables_for(pm_batch* b, int n) {
@@ -435,7 +453,9 @@ int build_plan(pm_batch* b, cudaStream_t st) {
       if (b->plan_host[t]) cudaFreeHost(b->plan_host[t]);
       b->plan_host[t] = nullptr;
       b->plan_host_bytes[t] = 0;
-      const size_t want = std::max(total, (size_t)64 << 10);
+      // doubled, so that a batch whose simulation count creeps up reallocates rarely: each
+      // cudaFreeHost synchronises the device, and the serving loop re-plans at every admission
+      const size_t want = std::max(2 * total, (size_t)256 << 10);
       PB_CK(cudaMallocHost(&b->plan_host[t], want), "alloc staging");
       b->plan_host_bytes[t] = want;
     }
@@ -475,7 +495,7 @@ int build_plan(pm_batch* b, cudaStream_t st) {
     if (kt != g_kick_cps.end()) P.kick_cps = kt->second;
     else b->tuned = false;
   }
-  drop_graphs(b);
+  b->host_s[1] -= drop_graphs(b);  // (counted as graph work, not planning)
   b->dirty = false;
   b->plan_steps = 0;
   return PM_OK;
@@ -745,7 +765,7 @@ int autotune(pm_batch* b, cudaStream_t st) {
     if (!kick_known) g_kick_cps[kkey] = P.kick_cps;
   }
   b->tuned = true;
-  drop_graphs(b);
+  b->host_s[4] -= drop_graphs(b);  // (counted as graph work, not tuning)
   return PM_OK;
 }
 
@@ -762,7 +782,7 @@ int run_steps(pm_batch* b, int k, cudaStream_t st) {
   for (int i = 0; i < k; ++i) {
     const int cur = b->cur;
     if (b->graphs && !b->sparse) {
-      if (!b->gexec[cur]) {
+      if (!b->gexec[cur] || b->gstale[cur]) {
         HostTimer timer(b->host_s[2]);
         cudaGraph_t g = nullptr;
         PB_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
@@ -773,7 +793,17 @@ int run_steps(pm_batch* b, int k, cudaStream_t st) {
           return r;
         }
         PB_CK(e, "end capture");
-        cudaError_t ie = cudaGraphInstantiate(&b->gexec[cur], g, 0);
+        cudaError_t ie = cudaSuccess;
+        if (b->gexec[cur]) {  // stale: update in place when the graph's shape allows it
+          cudaGraphExecUpdateResultInfo info;
+          if (cudaGraphExecUpdate(b->gexec[cur], g, &info) != cudaSuccess) {
+            cudaGetLastError();  // (not sticky: the shape changed)
+            cudaGraphExecDestroy(b->gexec[cur]);
+            b->gexec[cur] = nullptr;
+          }
+        }
+        if (!b->gexec[cur]) ie = cudaGraphInstantiate(&b->gexec[cur], g, 0);
+        b->gstale[cur] = false;
         cudaGraphDestroy(g);
         PB_CK(ie, "instantiate");
       }
@@ -884,7 +914,7 @@ int pm_batch_create(int device, size_t mem_cap_bytes, pm_batch** out) {
 
 void pm_batch_destroy(pm_batch* b) {
   if (!b) return;
-  drop_graphs(b);
+  drop_graphs(b, true);
   for (int w = 0; w < 2; ++w)
     for (int k = 0; k < kStateArrays; ++k) b->st[w][k].release();
   for (auto& s : b->sims) {
@@ -936,7 +966,7 @@ const char* pm_batch_last_error(const pm_batch* b) { return b ? b->err.c_str() :
 int pm_batch_set_graphs(pm_batch* b, int enable) {
   if (!b) return PM_ERR_ARG;
   b->graphs = enable != 0;
-  drop_graphs(b);
+  drop_graphs(b, true);
   return PM_OK;
 }
 
