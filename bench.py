@@ -576,6 +576,45 @@ def run_gradient(args, local):
     print(json.dumps(line), flush=True)
 
 
+def run_sizes(args, local):
+    """Per grid size: a batch of one size, particles on a grid twice as fine and the README
+    workload's resolution (box 250 N_PARTS / 256 Mpc/h), about 16.8M particles in all; the CUDA
+    event time of each phase of a step after --warmup steps (default 20 here), and its
+    achieved GB/s on the phase's algorithmic bytes."""
+    import pmgpu
+    import torch
+    from pmgpu.batch import Batch
+    from pmgpu.config import Config
+    from pmgpu.device_ics import DeviceICs
+    torch.cuda.set_device(local)
+    pmgpu.build()
+    peak, _ = measured_peak()
+    rows = []
+    for npart, count in ((32, 96), (48, 64), (64, 48), (96, 19), (128, 8), (192, 3), (256, 1)):
+        gen = DeviceICs(npart, local)
+        b = Batch(device=local)
+        for s in range(count):
+            c = Config(n_parts=npart, n_cells=2 * npart, box_size=250.0 * npart / 256, random_seed=s, steps=1000)
+            p, v = gen.generate(c)
+            b.add(c, p, v)
+        gen.close()
+        b.step(max(args.warmup, 20))
+        prof = b.profile(5)
+        b.check_device()
+        n, np_ = 2 * npart, count * npart ** 3
+        alg = {k: v * count for k, v in algorithmic_bytes(npart ** 3, n).items()}  # per simulation, times count
+        phases = {k: {"ms": round(v, 4), **({"gbs": round(alg[k] / (v / 1e3) / 1e9),
+                                              "frac": round(alg[k] / (v / 1e3) / 1e9 / peak, 3)}
+                                             if alg.get(k, 0) > 0 and v > 0 else {})}
+                  for k, v in prof.items() if v > 0.003}
+        rows.append({"n_cells": n, "sims": count, "particles": np_, "step_ms": round(sum(prof.values()), 4),
+                     "ns_per_particle": round(sum(prof.values()) * 1e6 / np_, 4), "phases": phases,
+                     "schedule": b.schedule()[0]})
+        b.close()
+    print(json.dumps({"metric": METRIC, "workload": "sizes", "unit": "ms per phase", "peak_gbs": peak,
+                      "rows": rows}), flush=True)
+
+
 def run_reference(args, ws, rank):
     """The reference's step on the host cores (its CPU port, see cpu_baseline): W untimed
     full-size steps, then the K timed steps the command asks for, on the same workload and
@@ -616,7 +655,7 @@ def main():
     ap.add_argument("--n-parts", type=int, default=256, help="reduced cases for profiling only")
     ap.add_argument("--n-cells", type=int, default=512)
     ap.add_argument("--box", type=float, default=250.0)
-    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served", "gradient"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served", "gradient", "sizes"],
                     help="plain: the README workload (headline); batched / served: the ensemble and "
                          "request-stream workloads")
     ap.add_argument("--batch-sims", type=int, default=64)
@@ -645,6 +684,9 @@ def main():
     elif args.workload == "gradient":
         if rank == 0:
             run_gradient(args, local)
+    elif args.workload == "sizes":
+        if rank == 0:
+            run_sizes(args, local)
     else:
         run_gpu(args, ws, rank, local)
 
