@@ -179,7 +179,12 @@ template <bool INV> struct DFT<24, INV> {
 };
 
 // ---------------------------------------------------------------------------------
-// Radix plans (product of radices == L)
+// Radix plans (product of radices == L).  Fewer passes mean fewer shared-memory round trips:
+// the two-pass plans of 128, 192, 256 and 384 and the three-pass plan of 1024 measured, per
+// 134M cells (y, z in ms), 128: 0.191, 0.311 -> 0.174, 0.265; 192: 0.243, 0.497 -> 0.228,
+// 0.335; 256: 0.208, 0.340 -> 0.190, 0.281; 384: 0.304, 0.843 -> 0.243, 0.631; 1024 (y, per
+// 1.07G cells): 1.88 -> 1.51.  512 keeps three radix-8 passes on pairs of lines (16 x 32 line
+// by line: z 0.291 -> 0.303 ms, half the threads idle in the radix-32 pass).
 // ---------------------------------------------------------------------------------
 template <int L> struct Plan;
 #define PM_PLAN(L_, ...)                                   \
@@ -195,13 +200,13 @@ PM_PLAN(32, 4, 8)
 PM_PLAN(48, 3, 4, 4)
 PM_PLAN(64, 8, 8)
 PM_PLAN(96, 3, 4, 8)
-PM_PLAN(128, 2, 8, 8)
-PM_PLAN(192, 3, 8, 8)
-PM_PLAN(256, 4, 8, 8)
-PM_PLAN(384, 3, 2, 8, 8)
+PM_PLAN(128, 8, 16)
+PM_PLAN(192, 12, 16)
+PM_PLAN(256, 16, 16)
+PM_PLAN(384, 24, 16)
 PM_PLAN(512, 8, 8, 8)
 PM_PLAN(768, 3, 4, 8, 8)
-PM_PLAN(1024, 2, 8, 8, 8)
+PM_PLAN(1024, 16, 8, 8)
 #undef PM_PLAN
 
 template <int LS>
@@ -277,10 +282,10 @@ __device__ __forceinline__ void fft_passes(float2* s, const float2* __restrict__
   }
 }
 
-// Lengths whose blocked transforms run on pairs of lines: all but the radix-3 plans other
-// than 192 and 384, whose tasks per pair overflow the registers (96 and 768 spill; 192 and
-// 384 on pairs measured 0.58 -> 0.50 and 0.91 -> 0.79 ms per 134M-cell z pass).
-__host__ __device__ constexpr bool blocked_pairs(int L) { return L % 3 != 0 || L == 192 || L == 384; }
+// Lengths whose blocked transforms run on pairs of lines: the plans of radix 8 or less, and
+// 128 (8 x 16).  The radix-12/16/24 plans hold too many values per pair of lines and run
+// line by line (on pairs they spill).
+__host__ __device__ constexpr bool blocked_pairs(int L) { return L % 3 != 0 && L != 256 && L != 1024; }
 
 // Whether task j of a stride-1 pass over NP pairs of lines stores its R outputs in the order
 // r ^ 1: with 4 pairs, the 8 lanes of a quarter-warp (one phase of a 128-bit shared-memory
