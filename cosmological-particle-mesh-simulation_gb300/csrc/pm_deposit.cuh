@@ -7,6 +7,8 @@
 // tile's particle count allows, else a low word and a coarse word).  Integer sums do not
 // depend on the order of the atomics, so the deposit is bit-identical run to run.
 #pragma once
+#include <type_traits>
+
 #include "pm_cells.cuh"
 
 namespace pm {
@@ -122,18 +124,50 @@ __device__ __forceinline__ void deposit_entry(unsigned* lo, unsigned* hi, int n,
 //   2-5: the tile below in y, its last row of each plane    6: the diagonal tile, last row
 constexpr int NRUN = 7;
 
-// Slot of source entry f (0xffffffff past the end): its run, its place in the row-sorted
-// order, and the permutation.
-__device__ __forceinline__ unsigned source_slot(const unsigned* __restrict__ perm, const unsigned* s_begin,
-                                                const unsigned* s_off, unsigned f, unsigned total) {
-  if (f >= total) return 0xffffffffu;
-  int r = 0;  // last run with s_off[r] <= f
-  if (s_off[4] <= f) r = 4;
-  if (s_off[r + 2] <= f) r += 2;
-  if (r + 1 < NRUN && s_off[r + 1] <= f) r += 1;
-  const unsigned pos = s_begin[r] + (f - s_off[r]);
-  return perm ? __ldg(&perm[pos]) : pos;  // no permutation: the state is in row order
-}
+// The run table of a tile: source entry f belongs to the last run r with off[r] <= f, and
+// sits at place f + delta[r] (= begin[r] + f - off[r]) of the row-sorted order.
+//
+// RunTable searches the table in shared memory (a chain of dependent loads before the
+// permutation load can issue, but no registers); RunRegs holds it in 14 registers and finds
+// the run with compares and selects.  The fused deposit takes RunRegs (0.535 -> 0.521 ms early,
+// 0.716 -> 0.636 ms at step 980, 256^3 on 512^3); the standalone deposit, at 40 registers a
+// thread, keeps RunTable.
+struct RunTable {
+  const unsigned *begin, *off;
+  __device__ __forceinline__ RunTable(const unsigned* s_begin, const unsigned* s_off) : begin(s_begin), off(s_off) {}
+  // Slot of source entry f (0xffffffff past the end): its place in the row-sorted order,
+  // through the permutation when there is one (else the state is in row order).
+  __device__ __forceinline__ unsigned slot(const unsigned* __restrict__ perm, unsigned f, unsigned total) const {
+    if (f >= total) return 0xffffffffu;
+    int r = 0;  // last run with off[r] <= f
+    if (off[4] <= f) r = 4;
+    if (off[r + 2] <= f) r += 2;
+    if (r + 1 < NRUN && off[r + 1] <= f) r += 1;
+    const unsigned pos = begin[r] + (f - off[r]);
+    return perm ? __ldg(&perm[pos]) : pos;
+  }
+};
+
+struct RunRegs {
+  unsigned off[NRUN], delta[NRUN];
+  __device__ __forceinline__ RunRegs(const unsigned* s_begin, const unsigned* s_off) {
+#pragma unroll
+    for (int r = 0; r < NRUN; ++r) {
+      off[r] = s_off[r];
+      delta[r] = s_begin[r] - s_off[r];
+    }
+  }
+  // Slot of source entry f (0xffffffff past the end): its place in the row-sorted order,
+  // through the permutation when there is one (else the state is in row order).
+  __device__ __forceinline__ unsigned slot(const unsigned* __restrict__ perm, unsigned f, unsigned total) const {
+    if (f >= total) return 0xffffffffu;
+    unsigned d = delta[0];
+#pragma unroll
+    for (int r = 1; r < NRUN; ++r) d = f >= off[r] ? delta[r] : d;
+    const unsigned pos = f + d;
+    return perm ? __ldg(&perm[pos]) : pos;
+  }
+};
 
 // Base cell of a source particle relative to the tile, from its loaded words; false if
 // absent or bad.  NN: the grid size when known at compile time (0: S.n).
@@ -212,13 +246,15 @@ __device__ __forceinline__ void deposit_sources(const Sim& S, const Parts& p, co
                                                 float qscale, int tid) {
   const int lane = tid & 31, warp = tid >> 5;
   const int n = NN ? NN : S.n;
+  using Runs = typename std::conditional<NN != 0, RunRegs, RunTable>::type;
+  const Runs runs(s_begin, s_off);
   unsigned base = (unsigned)warp * 32u;
-  unsigned sl0 = source_slot(perm, s_begin, s_off, base + lane, total);
-  unsigned sl1 = source_slot(perm, s_begin, s_off, base + NT + lane, total);
+  unsigned sl0 = runs.slot(perm, base + lane, total);
+  unsigned sl1 = runs.slot(perm, base + NT + lane, total);
   for (; base < total; base += 2 * NT) {
     const RawCell q0 = load_raw_cell<MODE>(p, sl0), q1 = load_raw_cell<MODE>(p, sl1);
-    sl0 = source_slot(perm, s_begin, s_off, base + 2 * NT + lane, total);
-    sl1 = source_slot(perm, s_begin, s_off, base + 3 * NT + lane, total);
+    sl0 = runs.slot(perm, base + 2 * NT + lane, total);
+    sl1 = runs.slot(perm, base + 3 * NT + lane, total);
     Cell c0, c1;
     int ly0 = 0, lz0 = 0, ly1 = 0, lz1 = 0;
     const bool ok0 = source_cell<MODE, NN>(S, p, q0, y0, z0, err, c0, ly0, lz0);
