@@ -76,7 +76,10 @@ struct Plan {
   long long sort_n = 0;  // slots the next step's sort reads (> ptot right after a retirement)
 };
 
-const int kStateArrays = 11;  // x y z vx vy vz id, cell record: cell fx fy fz
+// x y z vx vy vz id (4 bytes a particle each) and the cell record (16 bytes)
+const int kStateArrays = 8;
+constexpr size_t state_elem_bytes(int k) { return k == 7 ? 16 : 4; }
+constexpr size_t kStateBytes = 7 * 4 + 16;  // per particle
 
 // Schedules found by the autotuner, for the whole process: per (grid size, volume class of the
 // size's deposit tiles in the batch), and the kick's per volume class of its work units; a
@@ -182,10 +185,7 @@ Parts state(pm_batch* b, int which) {
   p.vy = b->st[which][4].as<float>();
   p.vz = b->st[which][5].as<float>();
   p.id = b->st[which][6].as<unsigned>();
-  p.cell = b->st[which][7].as<unsigned>();
-  p.fx = b->st[which][8].as<float>();
-  p.fy = b->st[which][9].as<float>();
-  p.fz = b->st[which][10].as<float>();
+  p.rec = b->st[which][7].as<uint4>();
   return p;
 }
 
@@ -201,7 +201,7 @@ size_t footprint(const pm_config& c) {
   size_t f = n * n * n * sizeof(float);                          // potential / density
   if (c.flags & PM_FLAG_KEEP_DENSITY) f += n * n * n * sizeof(float);
   f += n * n * (size_t)spec_pitch((int)n) * sizeof(float2);      // spectrum
-  f += np * (2 * kStateArrays * 4 + 4 * 4);                      // state x2, keys/vals x2
+  f += np * (2 * kStateBytes + 4 * 4);                           // state x2, keys/vals x2
   f += np * 6 * sizeof(float);                                   // final state
   f += 3 * n * n * sizeof(unsigned) + 4096;                      // row starts, counts, cursors, tables
   return f;
@@ -262,10 +262,10 @@ cudaError_t grow_state(pm_batch* b, long long need) {
   for (int w = 0; w < 2; ++w) {
     for (int k = 0; k < kStateArrays; ++k) {
       DBuf nb;
-      e = nb.ensure((size_t)cap * 4);
+      e = nb.ensure((size_t)cap * state_elem_bytes(k));
       if (e) return e;
       if (w == b->cur && keep > 0 && b->st[w][k].p) {
-        e = cudaMemcpy(nb.p, b->st[w][k].p, (size_t)keep * 4, cudaMemcpyDeviceToDevice);
+        e = cudaMemcpy(nb.p, b->st[w][k].p, (size_t)keep * state_elem_bytes(k), cudaMemcpyDeviceToDevice);
         if (e) return e;
       }
       b->st[w][k].release();

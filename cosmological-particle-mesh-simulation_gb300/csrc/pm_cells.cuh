@@ -90,31 +90,30 @@ __device__ __forceinline__ Cell cell_disp(const Sim& S, unsigned id, float dx, f
 constexpr unsigned CELL_BAD = 0xffffffffu;
 
 __device__ __forceinline__ void store_cell_record(const Parts& p, long long i, const Cell& c) {
-  p.cell[i] = c.ok ? ((unsigned)c.x | ((unsigned)c.y << 10) | ((unsigned)c.z << 20)) : CELL_BAD;
-  p.fx[i] = c.fx;
-  p.fy[i] = c.fy;
-  p.fz[i] = c.fz;
+  p.rec[i] = make_uint4(c.ok ? ((unsigned)c.x | ((unsigned)c.y << 10) | ((unsigned)c.z << 20)) : CELL_BAD,
+                        __float_as_uint(c.fx), __float_as_uint(c.fy), __float_as_uint(c.fz));
 }
 
-__device__ __forceinline__ Cell load_cell_record(const Parts& p, long long i) {
+__device__ __forceinline__ Cell record_cell(const uint4& v) {
   Cell c;
-  const unsigned k = p.cell[i];
-  c.ok = k != CELL_BAD;
-  c.x = (int)(k & 1023u);
-  c.y = (int)((k >> 10) & 1023u);
-  c.z = (int)((k >> 20) & 1023u);
-  c.fx = p.fx[i];
-  c.fy = p.fy[i];
-  c.fz = p.fz[i];
+  c.ok = v.x != CELL_BAD;
+  c.x = (int)(v.x & 1023u);
+  c.y = (int)((v.x >> 10) & 1023u);
+  c.z = (int)((v.x >> 20) & 1023u);
+  c.fx = __uint_as_float(v.y);
+  c.fy = __uint_as_float(v.z);
+  c.fz = __uint_as_float(v.w);
   return c;
 }
+
+__device__ __forceinline__ Cell load_cell_record(const Parts& p, long long i) { return record_cell(p.rec[i]); }
 
 // The base cell of a particle: from its absolute position, its cell record, or its
 // displacement (POS_DISP without records).
 template <int MODE>
 __device__ __forceinline__ Cell particle_cell(const Sim& S, const Parts& p, long long slot) {
   if (MODE == POS_ABS) return cell_abs(p.x[slot], p.y[slot], p.z[slot], S.n);
-  if (p.cell) return load_cell_record(p, slot);
+  if (p.rec) return load_cell_record(p, slot);
   return cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
 }
 
@@ -131,8 +130,9 @@ template <int MODE>
 __device__ __forceinline__ RawCell load_raw_cell(const Parts& p, unsigned slot) {
   RawCell r{0u, 0.f, 0.f, 0.f, slot != 0xffffffffu};
   if (!r.present) return r;
-  if (MODE == POS_DISP && p.cell) {
-    r.w = p.cell[slot]; r.a = p.fx[slot]; r.b = p.fy[slot]; r.c = p.fz[slot];
+  if (MODE == POS_DISP && p.rec) {
+    const uint4 v = __ldg(&p.rec[slot]);
+    r.w = v.x; r.a = __uint_as_float(v.y); r.b = __uint_as_float(v.z); r.c = __uint_as_float(v.w);
   } else {
     if (MODE == POS_DISP) r.w = p.id[slot];
     r.a = p.x[slot]; r.b = p.y[slot]; r.c = p.z[slot];
@@ -143,15 +143,7 @@ __device__ __forceinline__ RawCell load_raw_cell(const Parts& p, unsigned slot) 
 template <int MODE>
 __device__ __forceinline__ Cell raw_cell(const Sim& S, const Parts& p, const RawCell& r) {
   if (MODE == POS_ABS) return cell_abs(r.a, r.b, r.c, S.n);
-  if (p.cell) {
-    Cell c;
-    c.ok = r.w != CELL_BAD;
-    c.x = (int)(r.w & 1023u);
-    c.y = (int)((r.w >> 10) & 1023u);
-    c.z = (int)((r.w >> 20) & 1023u);
-    c.fx = r.a; c.fy = r.b; c.fz = r.c;
-    return c;
-  }
+  if (p.rec) return record_cell(make_uint4(r.w, __float_as_uint(r.a), __float_as_uint(r.b), __float_as_uint(r.c)));
   return cell_disp(S, r.w, r.a, r.b, r.c);
 }
 

@@ -120,11 +120,12 @@ struct Parts {
   float* x; float* y; float* z;       // positions (POS_ABS) or displacements (POS_DISP)
   float* vx; float* vy; float* vz;
   unsigned* id;                        // Lagrangian particle index (POS_DISP)
-  // cell record (POS_DISP, optional): base cell packed x | y << 10 | z << 20 (CELL_BAD if
-  // not finite) and the in-cell offsets, exactly as computed from the displacement; written
-  // with the state by the kick so that the deposit reads the cell instead of recomputing it
-  unsigned* cell;
-  float* fx; float* fy; float* fz;
+  // cell record (POS_DISP, optional), one 16-byte word per particle: the base cell packed
+  // x | y << 10 | z << 20 (CELL_BAD if not finite) and the bits of the three in-cell offsets,
+  // exactly as computed from the displacement.  The kick writes it with the state so that the
+  // deposit reads the cell instead of recomputing it, with one 16-byte load (four separate
+  // arrays measured 0.520 -> 0.485 ms per deposit, 256^3 on 512^3).
+  uint4* rec;
 };
 
 __device__ __forceinline__ int locate_sim(const Work& w, int unit) {

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(KEY_NT) k_keys(const Sim* __restrict__ sims, W
       c = cell_abs(x, y, z, S.n);
     } else {
       c = cell_disp(S, p.id[slot], p.x[slot], p.y[slot], p.z[slot]);
-      if (p.cell) store_cell_record(p, slot, c);
+      if (p.rec) store_cell_record(p, slot, c);
     }
     if (!c.ok) { set_error(err, ERR_CELL_RANGE); c.x = c.y = c.z = 0; }
     keys[slot] = cell_key(S, c);
@@ -239,7 +239,7 @@ __device__ __forceinline__ unsigned kick_store(const Sim& S, const Parts& out, l
     out.id[sp] = id;
     if (keys_next) {
       Cell cn = cell_disp(S, id, nx, ny, nz);
-      if (out.cell) store_cell_record(out, sp, cn);
+      if (out.rec) store_cell_record(out, sp, cn);
       if (!cn.ok) { set_error(err, ERR_CELL_RANGE); cn.x = cn.y = cn.z = 0; }
       const unsigned key = cell_key(S, cn);
       keys_next[sp] = key;
