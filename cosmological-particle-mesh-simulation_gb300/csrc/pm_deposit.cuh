@@ -280,13 +280,14 @@ __device__ __forceinline__ void deposit_sources(const Sim& S, const Parts& p, co
 // runs_ready.  Done by NT threads, tid = 0 .. NT - 1 (a whole CTA, or a group of its warps
 // with one tile each: every group calls it together, it synchronises the whole CTA).  Returns
 // how the sums are held (tile_sum), also written to *ts_out when given.  NN: the grid size
-// when known at compile time (0: S.n).
+// when known at compile time (0: S.n).  zeroed: lo (and hi) are already zero, so the zeroing
+// phase and its barrier are skipped.
 template <int MODE, int NT, int NN = 0>
 __device__ __forceinline__ TileSum deposit_tile(const Sim& S, const Parts& p, const unsigned* __restrict__ perm,
                                                 const unsigned* __restrict__ row_start, int* err, int y0, int z0,
                                                 unsigned* lo, unsigned* hi, int rs, unsigned* s_begin,
                                                 unsigned* s_off, bool runs_ready = false, int tid = -1,
-                                                TileSum* ts_out = nullptr) {
+                                                TileSum* ts_out = nullptr, bool zeroed = false) {
   if (tid < 0) tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
   const int n = NN ? NN : S.n;
@@ -298,13 +299,15 @@ __device__ __forceinline__ TileSum deposit_tile(const Sim& S, const Parts& p, co
   const TileSum ts = tile_sum(total, S.mass_scale);
   if (ts_out && tid == 0) *ts_out = ts;  // visible to the whole CTA after the barrier below
   // zero the rows of lo (and of hi for two-word sums), 4 words per store
-  const int q4 = n / 4;
-  for (int i = tid; i < TZ * TY * q4; i += NT) {
-    const int off = (i / q4) * rs + (i % q4) * 4;
-    *reinterpret_cast<uint4*>(lo + off) = make_uint4(0u, 0u, 0u, 0u);
-    if (!ts.s) *reinterpret_cast<uint4*>(hi + off) = make_uint4(0u, 0u, 0u, 0u);
+  if (!zeroed) {
+    const int q4 = n / 4;
+    for (int i = tid; i < TZ * TY * q4; i += NT) {
+      const int off = (i / q4) * rs + (i % q4) * 4;
+      *reinterpret_cast<uint4*>(lo + off) = make_uint4(0u, 0u, 0u, 0u);
+      if (!ts.s) *reinterpret_cast<uint4*>(hi + off) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __syncthreads();
   }
-  __syncthreads();
   if (ts.s)
     deposit_sources<MODE, NT, true, NN>(S, p, perm, err, y0, z0, lo, hi, rs, s_begin, s_off, total,
                                     __uint_as_float((unsigned)(127 + ts.s) << 23), tid);

@@ -846,13 +846,17 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), dep_ctas_bound(N))
       const int tj = lane < TPB * 8 ? lane >> 3 : 0;
       run_table(v, lane, s_begin[tj], s_off[tj], lane < TPB * 8);
     }
+    // The accumulators start zero, and each row is zeroed again by its transform lanes once
+    // they are done with it, so a tile needs no zeroing phase and barrier of its own
+    // (0.468 -> 0.460 ms early, 0.604 -> 0.587 ms at step 980, 256^3 on 512^3).
+    for (int i = threadIdx.x; i < TPB * NL * RS / 4; i += NT) acc_raw[i] = make_uint4(0u, 0u, 0u, 0u);
     __syncthreads();
     while (idx < w.total) {
       {  // the particles of this group's tile (a group without a tile has an empty table)
         int si, y0, z0;
         tile_of(idx + g, si, y0, z0);
         deposit_tile<MODE, NTT, N>(sims[si], p, perm, row_start, err, y0, z0, lo + g * NL * RS, hi + g * NL * RS, RS,
-                                s_begin[g], s_off[g], true, gtid, &s_ts[g]);
+                                s_begin[g], s_off[g], true, gtid, &s_ts[g], true);
       }
       // the CTA's TPB * NL rows: T lanes per row, rows R = warp * RPW + sub; a row's exchange
       // buffer overlays its own accumulator words once they are read
@@ -887,6 +891,15 @@ __global__ void __launch_bounds__(deposit_r2c_nt(N), dep_ctas_bound(N))
         if (thas) {
           const long long row = (long long)(tz0 + r / TY) * N + (ty0 + r % TY);
           xrow_untangle_store<N>(o2, rb, t, S.tw, S.spec + row * S.pitch);
+        }
+        __syncwarp();  // the row's lanes are done with its words
+        {  // zero what this tile dirtied: the low words and the exchange buffer (which reaches
+           // into the high words), and the high words after a two-word tile
+          constexpr int XW = 2 * Q * (P + 1);  // words of the exchange buffer
+          static_assert(XW % 4 == 0 && RS % 4 == 0, "rows zeroed 4 words at a time");
+          const int zw = ts.s ? (XW > N ? XW : N) : RS;
+          uint4* z4 = reinterpret_cast<uint4*>(lo + R * RS);
+          for (int i = t; i < zw / 4; i += T) z4[i] = make_uint4(0u, 0u, 0u, 0u);
         }
         if (warp == 0 && next < w.total) {
           const int tj = lane < TPB * 8 ? lane >> 3 : 0;
