@@ -165,9 +165,7 @@ __device__ __forceinline__ void cic_weights(const Cell& c, float w[8]) {
   w[6] = tx * c.fy * c.fz;
   w[7] = c.fx * c.fy * c.fz;
 }
-// corner offsets (ox, oy, oz) of the weights above
-__host__ __device__ constexpr int corner_x(int k) { return k == 1 || k == 4 || k == 5 || k == 7; }
-__host__ __device__ constexpr int corner_y(int k) { return k == 2 || k == 4 || k == 6 || k == 7; }
-__host__ __device__ constexpr int corner_z(int k) { return k == 3 || k == 5 || k == 6 || k == 7; }
+// (corner offsets (ox, oy, oz) of the weights above: 0 (0,0,0), 1 (1,0,0), 2 (0,1,0), 3 (0,0,1),
+// 4 (1,1,0), 5 (1,0,1), 6 (0,1,1), 7 (1,1,1))
 
 }  // namespace pm
