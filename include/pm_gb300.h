@@ -180,9 +180,10 @@ const char* pm_batch_last_error(const pm_batch* b);
 size_t pm_sim_footprint(const pm_config* cfg);
 /* Admits a simulation from absolute positions/velocities (3, N_PARTS^3) at cfg->a_init;
    on_device selects device or host input arrays (device arrays must be complete: work that
-   writes them on another stream has finished).  The arrays are no longer used when this
-   returns.  It waits for the steps already enqueued, not for the device as a whole.
-   PM_ERR_ADMIT if over the cap. */
+   writes them on another stream has finished).  The state is stored in the row order of the
+   particles' cells (a counting sort of their rows), as every later step leaves it.  The arrays
+   are no longer used when this returns.  It waits for the steps already enqueued, not for the
+   device as a whole.  PM_ERR_ADMIT if over the cap. */
 int pm_batch_add(pm_batch* b, const pm_config* cfg, const float* positions,
                  const float* velocities, int on_device, int* sim_id);
 /* 1 if pm_batch_add of this configuration would pass the memory cap now, else 0. */
